@@ -1,0 +1,183 @@
+// Shared device definitions for the GB300 multigrid curl-curl solver.
+//
+// Field layout (identical to the reference so the C ABI takes its buffers
+// as they are): 3 components, each on (n1+1)(n2+1)(n3+1) slots, component-
+// major, i fastest (src/gmg.c:1780; index id1..id3 in src/inject_extract.c:18).
+// A batch of right-hand sides stores RHS after RHS: field[rhs][3][S].
+// Cell arrays (volume-weighted conductivities and inverse permeability) are
+// [rhs][4][n3][n2][n1] in the order sigma11, sigma22, sigma33, invmur.
+// Per-RHS geometry is packed as 9 arrays of length nmax+1:
+//   x1 x2 x3 | ds1 ds2 ds3 | d1 d2 d3     (gmg.c:26-29, generate_xs_dx :1672)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace emmi {
+
+// ---------------------------------------------------------------- complex
+template <typename T> struct cplx;
+template <> struct cplx<float> { using type = float2; };
+template <> struct cplx<double> { using type = double2; };
+template <typename T> using C_t = typename cplx<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ C_t<T> mk(T re, T im) {
+  C_t<T> z; z.x = re; z.y = im; return z;
+}
+template <typename T> __device__ __forceinline__ C_t<T> cadd(C_t<T> a, C_t<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ C_t<T> csub(C_t<T> a, C_t<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ C_t<T> cmul(C_t<T> a, C_t<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ C_t<T> cscale(C_t<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+// a - b*c
+template <typename T> __device__ __forceinline__ C_t<T> cfms(C_t<T> a, C_t<T> b, C_t<T> c) {
+  return mk<T>(a.x - (b.x * c.x - b.y * c.y), a.y - (b.x * c.y + b.y * c.x));
+}
+// a - s*b (s real)
+template <typename T> __device__ __forceinline__ C_t<T> crfms(C_t<T> a, T s, C_t<T> b) {
+  return mk<T>(a.x - s * b.x, a.y - s * b.y);
+}
+// 1/z by the scaled formula conj(z)/|z|^2 with a power-of-two prescale so
+// |z|^2 neither overflows nor underflows (Smith-style range guard).
+template <typename T> __device__ __forceinline__ C_t<T> crcp(C_t<T> z) {
+  T m = fmax(fabs(z.x), fabs(z.y));
+  int e;
+  frexp(m, &e);
+  T zx = ldexp(z.x, -e), zy = ldexp(z.y, -e);
+  T inv = T(1) / (zx * zx + zy * zy);
+  return mk<T>(ldexp(zx * inv, -e), ldexp(-zy * inv, -e));
+}
+
+// ---------------------------------------------------------------- views
+// One multigrid level of a batch, in working precision T.
+template <typename T> struct LevelView {
+  int n[3];          // cells per direction
+  int nrhs;
+  long S;            // slots per component = (n1+1)(n2+1)(n3+1)
+  long ncell;        // n1*n2*n3
+  int gstride;       // per-RHS stride of geo (9*(gmax+1))
+  int gmax1;         // gmax+1: length of each packed geometry array
+  const T* geo;      // [nrhs][9][gmax+1]
+  const T* cells;    // [nrhs][4][ncell], volume weighted
+  C_t<T>* u;         // [nrhs][3][S]
+  C_t<T>* f;
+  C_t<T>* r;
+  const T* wmu;      // [nrhs] omega*mu0 (the operator's mass term is -i wmu sigma)
+  const int* active; // [nrhs] nonzero = work on this RHS (may be null)
+  const int* op;     // [nrhs] operator (geo/cells) index of each RHS (null: identity)
+};
+
+template <typename T> __device__ __forceinline__ int op_of(const LevelView<T>& L, int rhs) {
+  return L.op ? L.op[rhs] : rhs;
+}
+
+__host__ __device__ __forceinline__ long slot_id(const int n[3], int i, int j, int k) {
+  return i + (long)(n[0] + 1) * (j + (long)(n[1] + 1) * k);
+}
+__host__ __device__ __forceinline__ long cell_id(const int n[3], int i, int j, int k) {
+  return i + (long)n[0] * (j + (long)n[1] * k);
+}
+
+// geometry accessors: G[0..2]=x, G[3..5]=ds, G[6..8]=d
+template <typename T> struct Geo {
+  const T* g;
+  int len;
+  __device__ __forceinline__ const T* x(int e) const { return g + e * len; }
+  __device__ __forceinline__ const T* ds(int e) const { return g + (3 + e) * len; }
+  __device__ __forceinline__ const T* d(int e) const { return g + (6 + e) * len; }
+};
+
+// ---------------------------------------------------------------- stencil
+// Coefficients of the finite-integration curl-curl equation of the unknown
+// E_C at node indices P (src/gmg.c:1365-1404 in residual form, the matrix
+// rows of :199-318).  With p=(C+1)%3, q=(C+2)%3 and a,b,g the C-,p-,q-
+// indices:
+//   (A E)_C = (m1 T1/ds_p[b] - m2 T2/ds_p[b-1]) - (m3 T3/ds_q[g] - m4 T4/ds_q[g-1])
+//             - i wmu sbar E_C
+// expanded into one complex diagonal and 12 real neighbour coefficients in
+// the fixed order
+//   0 E_C(+p)  1 E_C(-p)  2 E_C(+q)  3 E_C(-q)
+//   4 E_p(+C)  5 E_p(0)   6 E_p(+C,-p)  7 E_p(-p)
+//   8 E_q(+C)  9 E_q(0)  10 E_q(+C,-q) 11 E_q(-q)
+// Entries with the same two cells are formed with identical operand order in
+// every row, so the assembled operator is exactly (bitwise) complex-symmetric.
+struct NbrOff { int comp; int dc, dp, dq; };
+
+template <int C> struct Cyc {
+  static constexpr int p = (C + 1) % 3;
+  static constexpr int q = (C + 2) % 3;
+};
+
+__host__ __device__ constexpr NbrOff nbr_off(int C, int k) {
+  // (component, offset along C, along p, along q)
+  return k == 0 ? NbrOff{C, 0, 1, 0}
+       : k == 1 ? NbrOff{C, 0, -1, 0}
+       : k == 2 ? NbrOff{C, 0, 0, 1}
+       : k == 3 ? NbrOff{C, 0, 0, -1}
+       : k == 4 ? NbrOff{(C + 1) % 3, 1, 0, 0}
+       : k == 5 ? NbrOff{(C + 1) % 3, 0, 0, 0}
+       : k == 6 ? NbrOff{(C + 1) % 3, 1, -1, 0}
+       : k == 7 ? NbrOff{(C + 1) % 3, 0, -1, 0}
+       : k == 8 ? NbrOff{(C + 2) % 3, 1, 0, 0}
+       : k == 9 ? NbrOff{(C + 2) % 3, 0, 0, 0}
+       : k == 10 ? NbrOff{(C + 2) % 3, 1, 0, -1}
+       : NbrOff{(C + 2) % 3, 0, 0, -1};
+}
+
+template <typename T> struct EdgeCoef {
+  T dre;   // real part of the diagonal (curl-curl)
+  T dim;   // imaginary part of the diagonal (-wmu * sbar)
+  T c[12];
+};
+
+// P[3]: node indices of the edge; strides of the cell array; G geometry.
+template <typename T, int C>
+__device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const T* __restrict__ sigC,
+                                          const T* __restrict__ imu, const Geo<T>& G, T wmu,
+                                          EdgeCoef<T>& e) {
+  constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
+  const int a = P[C], b = P[p], g = P[q];
+  const long cs[3] = {1, (long)n[0], (long)n[0] * n[1]};
+  const long c11 = a * cs[C] + (long)b * cs[p] + (long)g * cs[q];  // cell (p=b, q=g)
+  const long c10 = c11 - cs[q];                                     // (b, g-1)
+  const long c01 = c11 - cs[p];                                     // (b-1, g)
+  const long c00 = c01 - cs[q];                                     // (b-1, g-1)
+  const T s = T(0.25) * (((sigC[c00] + sigC[c01]) + sigC[c10]) + sigC[c11]);
+  const T i00 = imu[c00], i01 = imu[c01], i10 = imu[c10], i11 = imu[c11];
+  const T m1 = T(0.5) * (i11 + i10);  // H_q face at p=b
+  const T m2 = T(0.5) * (i01 + i00);  // H_q face at p=b-1
+  const T m3 = T(0.5) * (i11 + i01);  // H_p face at q=g
+  const T m4 = T(0.5) * (i10 + i00);  // H_p face at q=g-1
+  const T dc = G.ds(C)[a];
+  const T dpp = G.ds(p)[b], dpm = G.ds(p)[b - 1];
+  const T dqp = G.ds(q)[g], dqm = G.ds(q)[g - 1];
+  const T kpp = m1 / (dpp * dpp), kpm = m2 / (dpm * dpm);
+  const T kqp = m3 / (dqp * dqp), kqm = m4 / (dqm * dqm);
+  e.dre = (kpp + kpm) + (kqp + kqm);
+  e.dim = -wmu * s;
+  e.c[0] = -kpp;
+  e.c[1] = -kpm;
+  e.c[2] = -kqp;
+  e.c[3] = -kqm;
+  const T xp = m1 / (dc * dpp), xm = m2 / (dc * dpm);
+  const T yp = m3 / (dc * dqp), ym = m4 / (dc * dqm);
+  e.c[4] = xp;
+  e.c[5] = -xp;
+  e.c[6] = -xm;
+  e.c[7] = xm;
+  e.c[8] = yp;
+  e.c[9] = -yp;
+  e.c[10] = -ym;
+  e.c[11] = ym;
+}
+
+// slot offset of neighbour k of a component-C edge, in slot units, plus its
+// component's base offset (comp*S)
+template <int C>
+__device__ __forceinline__ long nbr_slot_delta(int k, const long ss[3], long S) {
+  const NbrOff o = nbr_off(C, k);
+  constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
+  return (long)o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
+}
+
+}  // namespace emmi

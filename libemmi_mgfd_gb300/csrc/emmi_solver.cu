@@ -1,0 +1,1131 @@
+// Batched multigrid solver for the curl-curl Maxwell system on GB300.
+//
+// A batch holds nrhs right-hand sides over nop operators (grid +
+// conductivity); all share n1 x n2 x n3.  The cycle structure is the
+// reference's (src/gmg.c:1586-1668, 1894-1932): F/V/W cycles, the level-0
+// residual-norm stopping test, and semi-coarsening whose uncoarsened
+// direction rotates with the cycle index (gmg.c:1755).  The three rotation
+// states give three fixed level hierarchies, built once at setup instead of
+// per cycle (gmg.c:1912), each captured into CUDA graphs:
+//   part A  = the work up to and including the level-0 residual and its norm
+//   part B  = the rest of the cycle
+// so the host can stop a right-hand side exactly where the reference would
+// (before the cycle's work) with one small device-to-host read per cycle.
+//
+// EMMI_PREC_FP64 runs the cycles in complex128 (the reference's arithmetic).
+// EMMI_PREC_MIXED runs them in complex64 on a preconditioner operator whose
+// conductivity is floored at sigma_floor (the air layer at 1e-8 S/m makes the
+// complex64 block solves unstable), and refines in FP64: x += e,
+// r = b - A x with the true operator in FP64, until |r| <= tol |b|.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "emmi_gpu.h"
+#include "emmi_kernels.cuh"
+
+using namespace emmi;
+
+namespace {
+
+thread_local std::string g_err;
+
+void set_err(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+#define CK(x)                                                                     \
+  do {                                                                            \
+    cudaError_t e_ = (x);                                                         \
+    if (e_ != cudaSuccess) {                                                      \
+      set_err("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));   \
+      return EMMI_ECUDA;                                                          \
+    }                                                                             \
+  } while (0)
+
+constexpr double kMu0 = 4. * 3.14159265358979323846264 * 1e-7;  // include/cstd.h:38-40
+constexpr int kMaxLev = 24;
+
+// gmg.c:1688-1699
+int depth_of(int n) {
+  int l = 0, nn = n;
+  while (nn % 2 == 0 && nn > 1) {
+    l++;
+    nn >>= 1;
+  }
+  if (nn > 2) l++;
+  return l;
+}
+
+// x -> xs, d, ds (gmg.c:1672-1685)
+void stagger(int n, const double* x, double* xs, double* d, double* ds) {
+  for (int i = 0; i < n; i++) {
+    ds[i] = x[i + 1] - x[i];
+    xs[i] = 0.5 * (x[i] + x[i + 1]);
+  }
+  xs[n] = x[n] + 0.5 * ds[n - 1];
+  ds[n] = xs[n] - x[n];
+  for (int i = 1; i <= n; i++) d[i] = xs[i] - xs[i - 1];
+  d[0] = xs[0] - x[0];
+}
+
+struct HLev {
+  int n[3];
+  int sc[3];
+  long S, ncell;
+};
+
+// ------------------------------------------------------------ setup kernels
+// cells64 = raw * vol, vol = d1s*d2s*d3s (gmg.c:1795-1799); sigmas floored at
+// `floor` (invmur untouched); also writes a float copy when c32 != null.
+__global__ void k_weight_cells(const float* __restrict__ raw, const double* __restrict__ geo,
+                               int gstride, int gmax1, int n0, int n1, int n2, double floor,
+                               double* __restrict__ c64, float* __restrict__ c32) {
+  const long ncell = (long)n0 * n1 * n2;
+  const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (id >= ncell) return;
+  const int op = blockIdx.y;
+  const int i = (int)(id % n0), j = (int)((id / n0) % n1), k = (int)(id / ((long)n0 * n1));
+  const double* g = geo + (long)op * gstride;
+  const double vol = g[3 * gmax1 + i] * g[4 * gmax1 + j] * g[5 * gmax1 + k];
+  for (int a = 0; a < 4; a++) {
+    double s = raw[((long)op * 4 + a) * ncell + id];
+    if (a < 3 && s < floor) s = floor;
+    const double v = s * vol;
+    if (c64) c64[((long)op * 4 + a) * ncell + id] = v;
+    if (c32) c32[((long)op * 4 + a) * ncell + id] = (float)v;
+  }
+}
+
+__global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// f = b * dual volume (gmg.c:1901-1910)
+__global__ void k_scale_dual(const double2* __restrict__ b, double2* __restrict__ f,
+                             const double* __restrict__ geo, const int* __restrict__ op, int gstride,
+                             int gmax1, int n0, int n1, int n2) {
+  const long S = (long)(n0 + 1) * (n1 + 1) * (n2 + 1);
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int rhs = blockIdx.y;
+  const int o = op ? op[rhs] : rhs;
+  const int i = (int)(s % (n0 + 1)), j = (int)((s / (n0 + 1)) % (n1 + 1)),
+            k = (int)(s / ((long)(n0 + 1) * (n1 + 1)));
+  const double* g = geo + (long)o * gstride;
+  const double d1s = g[3 * gmax1 + i], d2s = g[4 * gmax1 + j], d3s = g[5 * gmax1 + k];
+  const double d1 = g[6 * gmax1 + i], d2 = g[7 * gmax1 + j], d3 = g[8 * gmax1 + k];
+  const long base = (long)rhs * 3 * S;
+  const double w[3] = {d1s * d2 * d3, d1 * d2s * d3, d1 * d2 * d3s};
+  for (int c = 0; c < 3; c++) {
+    const double2 v = b[base + c * S + s];
+    f[base + c * S + s] = make_double2(v.x * w[c], v.y * w[c]);
+  }
+}
+
+// x64 += e32 on masked RHS
+__global__ void k_accumulate(double2* __restrict__ x, const float2* __restrict__ e, long n3s,
+                             const int* __restrict__ mask) {
+  const int rhs = blockIdx.y;
+  if (mask && !mask[rhs]) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n3s; i += (long)gridDim.x * blockDim.x) {
+    const float2 v = e[(long)rhs * n3s + i];
+    double2 a = x[(long)rhs * n3s + i];
+    a.x += (double)v.x;
+    a.y += (double)v.y;
+    x[(long)rhs * n3s + i] = a;
+  }
+}
+
+__global__ void k_zero_masked(float2* __restrict__ p, long n3s, const int* __restrict__ mask) {
+  const int rhs = blockIdx.y;
+  if (mask && !mask[rhs]) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n3s; i += (long)gridDim.x * blockDim.x)
+    p[(long)rhs * n3s + i] = make_float2(0.f, 0.f);
+}
+
+// H = curl E / (i wmu) on faces (gmg.c:1414-1460)
+__global__ void k_curl_h(const double2* __restrict__ E, double2* __restrict__ H,
+                         const double* __restrict__ geo, const int* __restrict__ op,
+                         const double* __restrict__ wmu, int gstride, int gmax1, int n0, int n1,
+                         int n2) {
+  const long S = (long)(n0 + 1) * (n1 + 1) * (n2 + 1);
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int rhs = blockIdx.y;
+  const int o = op ? op[rhs] : rhs;
+  const int i = (int)(s % (n0 + 1)), j = (int)((s / (n0 + 1)) % (n1 + 1)),
+            k = (int)(s / ((long)(n0 + 1) * (n1 + 1)));
+  const long base = (long)rhs * 3 * S;
+  if (i >= n0 || j >= n1 || k >= n2) {
+    for (int c = 0; c < 3; c++) H[base + c * S + s] = make_double2(0, 0);
+    return;
+  }
+  const double* g = geo + (long)o * gstride;
+  const double d1s = g[3 * gmax1 + i], d2s = g[4 * gmax1 + j], d3s = g[5 * gmax1 + k];
+  const long si = 1, sj = n0 + 1, sk = (long)(n0 + 1) * (n1 + 1);
+  const double2* Ex = E + base;
+  const double2* Ey = E + base + S;
+  const double2* Ez = E + base + 2 * S;
+  auto sub = [](double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); };
+  auto sc = [](double2 a, double d) { return make_double2(a.x / d, a.y / d); };
+  const double2 t1 = sub(sc(sub(Ez[s + sj], Ez[s]), d2s), sc(sub(Ey[s + sk], Ey[s]), d3s));
+  const double2 t2 = sub(sc(sub(Ex[s + sk], Ex[s]), d3s), sc(sub(Ez[s + si], Ez[s]), d1s));
+  const double2 t3 = sub(sc(sub(Ey[s + si], Ey[s]), d1s), sc(sub(Ex[s + sj], Ex[s]), d2s));
+  // t / (i w) = (t.y/w, -t.x/w)
+  const double w = wmu[rhs];
+  H[base + s] = make_double2(t1.y / w, -t1.x / w);
+  H[base + S + s] = make_double2(t2.y / w, -t2.x / w);
+  H[base + 2 * S + s] = make_double2(t3.y / w, -t3.x / w);
+}
+
+inline unsigned blocks_for(long n, int bs = 256, long cap = 65535) {
+  long b = (n + bs - 1) / bs;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+// ============================================================ solver state
+struct emmi_solver {
+  emmi_options opt;
+  int n[3];
+  int nop, nrhs, lmax;
+  int gmax1, gstride;
+  HLev hier[3][kMaxLev];
+  bool has_norm;  // the cycle has a level-0 norm test
+
+  // device memory
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+  int* d_op = nullptr;
+  int* d_active = nullptr;  // cycling RHS
+  int* d_refine = nullptr;  // RHS refining now (MIXED)
+  double* d_wmu64 = nullptr;
+  float* d_wmu32 = nullptr;
+  double* d_norm = nullptr;   // level-0 norm^2 per RHS (cycle)
+  double* d_norm64 = nullptr; // FP64 refinement norm^2 per RHS
+  double* geo64[3][kMaxLev] = {};
+  float* geo32[3][kMaxLev] = {};
+  double* cells64[3][kMaxLev] = {};
+  float* cells32[3][kMaxLev] = {};
+  double2 *u64[kMaxLev] = {}, *f64[kMaxLev] = {}, *r64[kMaxLev] = {};
+  float2 *u32[kMaxLev] = {}, *f32[kMaxLev] = {}, *r32[kMaxLev] = {};
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  int chunk = 1;  // RHS per line-sweep launch (scratch bound)
+
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t gA[3] = {}, gB[3] = {};
+  long nodesA[3] = {}, nodesB[3] = {};
+  double last_time = 0;
+  long last_launches = 0;
+  long launch_counter = 0;
+
+  // host mirrors
+  std::vector<int> h_active, h_refine;
+
+  template <typename T> LevelView<T> view(int h, int l) const;
+  template <typename T> void emit_smooth(int h, int l, int iter);
+  template <typename T> void emit_cycle(int h, int l, int kind, int want, int& cur);
+  template <typename T> void emit_residual0(int want, int& cur);
+  template <typename T> int build_graphs();
+  int alloc(void** p, size_t b);
+};
+
+int emmi_solver::alloc(void** p, size_t b) {
+  if (b == 0) b = 16;
+  cudaError_t e = cudaMalloc(p, b);
+  if (e != cudaSuccess) {
+    set_err("cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
+    return EMMI_ENOMEM;
+  }
+  allocs.push_back(*p);
+  bytes += b;
+  return EMMI_OK;
+}
+
+template <>
+LevelView<double> emmi_solver::view<double>(int h, int l) const {
+  LevelView<double> V;
+  const HLev& H = hier[h][l];
+  for (int e = 0; e < 3; e++) V.n[e] = H.n[e];
+  V.nrhs = nrhs;
+  V.S = H.S;
+  V.ncell = H.ncell;
+  V.gstride = gstride;
+  V.gmax1 = gmax1;
+  V.geo = geo64[h][l];
+  V.cells = cells64[h][l];
+  V.u = u64[l];
+  V.f = f64[l];
+  V.r = r64[l];
+  V.wmu = d_wmu64;
+  V.active = d_active;
+  V.op = d_op;
+  return V;
+}
+
+template <>
+LevelView<float> emmi_solver::view<float>(int h, int l) const {
+  LevelView<float> V;
+  const HLev& H = hier[h][l];
+  for (int e = 0; e < 3; e++) V.n[e] = H.n[e];
+  V.nrhs = nrhs;
+  V.S = H.S;
+  V.ncell = H.ncell;
+  V.gstride = gstride;
+  V.gmax1 = gmax1;
+  V.geo = geo32[h][l];
+  V.cells = cells32[h][l];
+  V.u = u32[l];
+  V.f = f32[l];
+  V.r = r32[l];
+  V.wmu = d_wmu32;
+  V.active = d_active;
+  V.op = d_op;
+  return V;
+}
+
+// smoothing (gmg.c:1301-1313): line relaxation along every direction the
+// next level coarsens, else node-patch relaxation; odd iter reverses colours
+template <typename T>
+void emmi_solver::emit_smooth(int h, int l, int iter) {
+  LevelView<T> V = view<T>(h, l);
+  const bool rev = iter % 2 == 1;
+  if (opt.isemicoarsen && l < lmax - 1) {
+    for (int d = 0; d < 3; d++) {
+      if (hier[h][l + 1].sc[d] != 2) continue;
+      for (int cc = 0; cc < 4; cc++) {
+        const int col = rev ? 3 - cc : cc;
+        for (int r0 = 0; r0 < nrhs; r0 += chunk) {
+          LevelView<T> W = V;
+          const int nr = std::min(chunk, nrhs - r0);
+          W.nrhs = nr;
+          W.u += (long)r0 * 3 * V.S;
+          W.f += (long)r0 * 3 * V.S;
+          W.r += (long)r0 * 3 * V.S;
+          W.wmu += r0;
+          W.active += r0;
+          W.op += r0;
+          launch_line_sweep<T>(W, d, col, (C_t<T>*)scratch, st);
+          launch_counter++;
+        }
+      }
+    }
+  } else {
+    for (int cc = 0; cc < 8; cc++) {
+      launch_point_sweep<T>(V, rev ? 7 - cc : cc, st);
+      launch_counter++;
+    }
+  }
+}
+
+// level-0 residual with norm: the point where the cycle tests convergence
+template <typename T>
+void emmi_solver::emit_residual0(int want, int& cur) {
+  if (cur == want) {
+    cudaMemsetAsync(d_norm, 0, nrhs * sizeof(double), st);
+    LevelView<T> V = view<T>(0, 0);
+    launch_residual<T, T>(V, V.r, d_norm, st);
+    launch_counter++;
+  }
+  cur = 1;
+}
+
+// kind: 1 V, 2 F, 3 W (gmg.c:1586-1668).  Emits only the launches of part
+// `want` (0 = before/including the level-0 norm, 1 = after it).
+template <typename T>
+void emmi_solver::emit_cycle(int h, int l, int kind, int want, int& cur) {
+  auto can_descend = [&](int lv) {
+    return lv < lmax - 1 && hier[h][lv + 1].sc[0] * hier[h][lv + 1].sc[1] * hier[h][lv + 1].sc[2] > 1;
+  };
+  auto to_coarse = [&](int lv) {
+    if (cur == want) {
+      launch_restrict<T>(view<T>(h, lv), view<T>(h, lv + 1), hier[h][lv + 1].sc, st);
+      launch_counter++;
+    }
+  };
+  auto to_fine = [&](int lv) {
+    if (cur == want) {
+      launch_prolong<T>(view<T>(h, lv), view<T>(h, lv + 1), hier[h][lv + 1].sc, st);
+      launch_counter++;
+    }
+  };
+  auto residual = [&](int lv) {
+    if (lv == 0 && kind == opt.cycleopt) {
+      emit_residual0<T>(want, cur);
+    } else if (cur == want) {
+      LevelView<T> V = view<T>(h, lv);
+      launch_residual<T, T>(V, V.r, nullptr, st);
+      launch_counter++;
+    }
+  };
+  auto smooth = [&](int lv, int it) {
+    if (cur == want) emit_smooth<T>(h, lv, it);
+  };
+  if (kind == 2) {  // F
+    if (l == lmax - 1) {
+      if (cur == want) {
+        LevelView<T> V = view<T>(h, l);
+        launch_zero<T>(V.u, 3 * V.S * nrhs, st);
+        launch_counter++;
+      }
+    } else if (can_descend(l)) {
+      residual(l);
+      to_coarse(l);
+      emit_cycle<T>(h, l + 1, 2, want, cur);
+      to_fine(l);
+    }
+    emit_cycle<T>(h, l, 1, want, cur);
+    return;
+  }
+  // V (kind 1) and W (kind 3)
+  for (int i = 0; i < opt.v1; i++) smooth(l, i);
+  if (can_descend(l)) {
+    residual(l);
+    to_coarse(l);
+    emit_cycle<T>(h, l + 1, kind, want, cur);
+    if (kind == 3) emit_cycle<T>(h, l + 1, kind, want, cur);
+    to_fine(l);
+  }
+  for (int i = 0; i < opt.v2; i++) smooth(l, i);
+}
+
+template <typename T>
+int emmi_solver::build_graphs() {
+  for (int h = 0; h < 3; h++) {
+    for (int part = 0; part < 2; part++) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      long before = launch_counter;
+      int cur = 0;
+      if (opt.cycleopt == 2) {
+        // F-cycle: the only level-0 residual of the top call is the norm one
+        emit_cycle<T>(h, 0, 2, part, cur);
+      } else {
+        emit_cycle<T>(h, 0, opt.cycleopt, part, cur);
+      }
+      CK(cudaStreamEndCapture(st, &g));
+      size_t nn = 0;
+      cudaGraphGetNodes(g, nullptr, &nn);
+      (part ? nodesB : nodesA)[h] = launch_counter - before;
+      CK(cudaGraphInstantiate(part ? &gB[h] : &gA[h], g, 0));
+      cudaGraphDestroy(g);
+    }
+  }
+  launch_counter = 0;
+  return EMMI_OK;
+}
+
+// ============================================================ C ABI
+extern "C" {
+
+const char* emmi_last_error(void) { return g_err.c_str(); }
+
+void emmi_default_options(emmi_options* o) {
+  o->cycleopt = 2;
+  o->ncycle = 30;
+  o->v1 = 1;
+  o->v2 = 1;
+  o->tol = 1e-6;
+  o->isemicoarsen = 1;
+  o->precision = EMMI_PREC_MIXED;
+  o->sigma_floor = 0;
+  o->refine_every = 3;
+  o->use_graphs = 1;
+  o->verb = 0;
+}
+
+int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_options* opts) {
+  if (!out || !P || !P->x1 || !P->x2 || !P->x3 || !P->cells || !P->omega) {
+    set_err("emmi_solver_create: null argument");
+    return EMMI_EINVAL;
+  }
+  if (P->n1 < 2 || P->n2 < 2 || P->n3 < 2 || P->nop < 1 || P->nrhs < 1) {
+    set_err("emmi_solver_create: bad sizes n=(%d,%d,%d) nop=%d nrhs=%d", P->n1, P->n2, P->n3,
+            P->nop, P->nrhs);
+    return EMMI_EINVAL;
+  }
+  if (P->op)
+    for (int r = 0; r < P->nrhs; r++)
+      if (P->op[r] < 0 || P->op[r] >= P->nop) {
+        set_err("emmi_solver_create: op[%d]=%d out of range", r, P->op[r]);
+        return EMMI_EINVAL;
+      }
+  if (!P->op && P->nop != P->nrhs) {
+    set_err("emmi_solver_create: op==NULL needs nop==nrhs");
+    return EMMI_EINVAL;
+  }
+  emmi_solver* s = new emmi_solver();
+  if (opts) s->opt = *opts; else emmi_default_options(&s->opt);
+  if (s->opt.refine_every < 1) s->opt.refine_every = 3;
+  if (s->opt.cycleopt < 1 || s->opt.cycleopt > 3) s->opt.cycleopt = 2;
+  s->n[0] = P->n1;
+  s->n[1] = P->n2;
+  s->n[2] = P->n3;
+  s->nop = P->nop;
+  s->nrhs = P->nrhs;
+  s->lmax = std::max(depth_of(P->n1), std::max(depth_of(P->n2), depth_of(P->n3)));
+  if (s->lmax < 1) s->lmax = 1;
+  if (s->lmax > kMaxLev) {
+    set_err("too many levels");
+    delete s;
+    return EMMI_EINVAL;
+  }
+  const int gmax = std::max(P->n1, std::max(P->n2, P->n3));
+  s->gmax1 = gmax + 1;
+  s->gstride = 9 * s->gmax1;
+  const bool mixed = s->opt.precision == EMMI_PREC_MIXED;
+  int rc;
+#define TRY(x)                 \
+  do {                         \
+    rc = (x);                  \
+    if (rc != EMMI_OK) {       \
+      emmi_solver_destroy(s);  \
+      return rc;               \
+    }                          \
+  } while (0)
+#define CKS(x)                                                                   \
+  do {                                                                           \
+    cudaError_t e_ = (x);                                                        \
+    if (e_ != cudaSuccess) {                                                     \
+      set_err("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));  \
+      emmi_solver_destroy(s);                                                    \
+      return EMMI_ECUDA;                                                         \
+    }                                                                            \
+  } while (0)
+  CKS(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+  CKS(cudaEventCreate(&s->ev0));
+  CKS(cudaEventCreate(&s->ev1));
+
+  // ---- hierarchies (grid_init, gmg.c:1744-1760)
+  for (int h = 0; h < 3; h++) {
+    HLev& L0 = s->hier[h][0];
+    for (int e = 0; e < 3; e++) {
+      L0.n[e] = s->n[e];
+      L0.sc[e] = 1;
+    }
+    for (int l = 1; l < s->lmax; l++) {
+      const HLev& F = s->hier[h][l - 1];
+      HLev& C = s->hier[h][l];
+      for (int e = 0; e < 3; e++) C.sc[e] = (F.n[e] % 2 == 0 && F.n[e] > 2) ? 2 : 1;
+      if (s->opt.isemicoarsen) C.sc[h] = 1;
+      for (int e = 0; e < 3; e++) C.n[e] = F.n[e] / C.sc[e];
+    }
+    for (int l = 0; l < s->lmax; l++) {
+      HLev& L = s->hier[h][l];
+      L.S = (long)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
+      L.ncell = (long)L.n[0] * L.n[1] * L.n[2];
+    }
+  }
+  // a non-semicoarsened batch has one hierarchy; keep three identical copies
+  s->has_norm = s->lmax > 1 && s->hier[0][1].sc[0] * s->hier[0][1].sc[1] * s->hier[0][1].sc[2] > 1;
+
+  // ---- geometry per (h, l, op) on the host, then upload
+  {
+    const size_t gsz = (size_t)s->nop * s->gstride;
+    std::vector<double> g64(gsz), prev(gsz);
+    std::vector<float> g32(gsz);
+    std::vector<double> xs_tmp(s->gmax1);
+    for (int h = 0; h < 3; h++) {
+      for (int l = 0; l < s->lmax; l++) {
+        const HLev& L = s->hier[h][l];
+        std::fill(g64.begin(), g64.end(), 0.0);
+        for (int o = 0; o < s->nop; o++) {
+          double* G = g64.data() + (size_t)o * s->gstride;
+          const double* Gp = prev.data() + (size_t)o * s->gstride;
+          for (int e = 0; e < 3; e++) {
+            double* x = G + e * s->gmax1;
+            if (l == 0) {
+              const float* src = e == 0 ? P->x1 : e == 1 ? P->x2 : P->x3;
+              for (int i = 0; i <= L.n[e]; i++) x[i] = (double)src[(size_t)o * (s->n[e] + 1) + i];
+            } else {
+              // coordinates by sub-sampling the finer level (gmg.c:1784-1786)
+              for (int i = 0; i <= L.n[e]; i++) x[i] = Gp[e * s->gmax1 + L.sc[e] * i];
+            }
+            stagger(L.n[e], x, xs_tmp.data(), G + (6 + e) * s->gmax1, G + (3 + e) * s->gmax1);
+          }
+        }
+        prev = g64;
+        if (h > 0 && l == 0) {
+          s->geo64[h][0] = s->geo64[0][0];
+          s->geo32[h][0] = s->geo32[0][0];
+          continue;
+        }
+        for (size_t i = 0; i < gsz; i++) g32[i] = (float)g64[i];
+        TRY(s->alloc((void**)&s->geo64[h][l], gsz * sizeof(double)));
+        TRY(s->alloc((void**)&s->geo32[h][l], gsz * sizeof(float)));
+        CKS(cudaMemcpy(s->geo64[h][l], g64.data(), gsz * sizeof(double), cudaMemcpyHostToDevice));
+        CKS(cudaMemcpy(s->geo32[h][l], g32.data(), gsz * sizeof(float), cudaMemcpyHostToDevice));
+      }
+    }
+  }
+
+  // ---- per-RHS scalars
+  {
+    std::vector<int> op(s->nrhs);
+    std::vector<double> w64(s->nrhs);
+    std::vector<float> w32(s->nrhs);
+    for (int r = 0; r < s->nrhs; r++) {
+      op[r] = P->op ? P->op[r] : r;
+      // I*omega*mu0 as gmg_init forms it (gmg.c:1710): imag = (double)omega_f * mu0
+      w64[r] = (double)P->omega[r] * kMu0;
+      w32[r] = (float)w64[r];
+    }
+    TRY(s->alloc((void**)&s->d_op, s->nrhs * sizeof(int)));
+    TRY(s->alloc((void**)&s->d_active, s->nrhs * sizeof(int)));
+    TRY(s->alloc((void**)&s->d_refine, s->nrhs * sizeof(int)));
+    TRY(s->alloc((void**)&s->d_wmu64, s->nrhs * sizeof(double)));
+    TRY(s->alloc((void**)&s->d_wmu32, s->nrhs * sizeof(float)));
+    TRY(s->alloc((void**)&s->d_norm, s->nrhs * sizeof(double)));
+    TRY(s->alloc((void**)&s->d_norm64, s->nrhs * sizeof(double)));
+    CKS(cudaMemcpy(s->d_op, op.data(), s->nrhs * sizeof(int), cudaMemcpyHostToDevice));
+    CKS(cudaMemcpy(s->d_wmu64, w64.data(), s->nrhs * sizeof(double), cudaMemcpyHostToDevice));
+    CKS(cudaMemcpy(s->d_wmu32, w32.data(), s->nrhs * sizeof(float), cudaMemcpyHostToDevice));
+    s->h_active.assign(s->nrhs, 1);
+    s->h_refine.assign(s->nrhs, 0);
+  }
+
+  // ---- cells: level 0 weighted by volume, coarse levels by summation
+  {
+    const long nc0 = s->hier[0][0].ncell;
+    float* raw = nullptr;
+    TRY(s->alloc((void**)&raw, (size_t)s->nop * 4 * nc0 * sizeof(float)));
+    CKS(cudaMemcpy(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float), cudaMemcpyHostToDevice));
+    // true operator in FP64 at level 0 (both modes)
+    TRY(s->alloc((void**)&s->cells64[0][0], (size_t)s->nop * 4 * nc0 * sizeof(double)));
+    dim3 g0(blocks_for(nc0), s->nop);
+    k_weight_cells<<<g0, 256, 0, s->st>>>(raw, s->geo64[0][0], s->gstride, s->gmax1, s->n[0], s->n[1],
+                                          s->n[2], -1.0, s->cells64[0][0], nullptr);
+    for (int h = 1; h < 3; h++) s->cells64[h][0] = s->cells64[0][0];
+    if (!mixed) {
+      for (int h = 0; h < 3; h++)
+        for (int l = 1; l < s->lmax; l++) {
+          const HLev& C = s->hier[h][l];
+          TRY(s->alloc((void**)&s->cells64[h][l], (size_t)s->nop * 4 * C.ncell * sizeof(double)));
+          launch_coarsen_cells<double>(s->cells64[h][l - 1], s->hier[h][l - 1].n, s->cells64[h][l],
+                                       C.sc, s->nop, s->st);
+        }
+    } else {
+      // preconditioner operator: floored conductivity, summed in FP64, stored f32
+      double floor = s->opt.sigma_floor;
+      if (floor <= 0) {
+        float wmin = P->omega[0];
+        for (int r = 1; r < s->nrhs; r++) wmin = std::min(wmin, P->omega[r]);
+        floor = 1e-4 * std::max(1.0, 2.0 * 3.14159265358979323846 / (double)wmin);
+      }
+      s->opt.sigma_floor = floor;
+      double* tmp[2] = {nullptr, nullptr};
+      TRY(s->alloc((void**)&tmp[0], (size_t)s->nop * 4 * nc0 * sizeof(double)));
+      TRY(s->alloc((void**)&tmp[1], (size_t)s->nop * 4 * nc0 * sizeof(double)));
+      TRY(s->alloc((void**)&s->cells32[0][0], (size_t)s->nop * 4 * nc0 * sizeof(float)));
+      k_weight_cells<<<g0, 256, 0, s->st>>>(raw, s->geo64[0][0], s->gstride, s->gmax1, s->n[0],
+                                            s->n[1], s->n[2], floor, tmp[0], s->cells32[0][0]);
+      for (int h = 1; h < 3; h++) s->cells32[h][0] = s->cells32[0][0];
+      for (int h = 0; h < 3; h++) {
+        int cur = 0;
+        for (int l = 1; l < s->lmax; l++) {
+          const HLev& C = s->hier[h][l];
+          const double* src = (l == 1) ? tmp[0] : tmp[cur];
+          double* dst = (l == 1) ? tmp[1] : tmp[1 - cur];
+          launch_coarsen_cells<double>(src, s->hier[h][l - 1].n, dst, C.sc, s->nop, s->st);
+          TRY(s->alloc((void**)&s->cells32[h][l], (size_t)s->nop * 4 * C.ncell * sizeof(float)));
+          const long nn = (long)s->nop * 4 * C.ncell;
+          k_d2f<<<blocks_for(nn), 256, 0, s->st>>>(dst, s->cells32[h][l], nn);
+          cur = (l == 1) ? 1 : 1 - cur;
+        }
+      }
+      CKS(cudaStreamSynchronize(s->st));
+    }
+    CKS(cudaGetLastError());
+    CKS(cudaStreamSynchronize(s->st));
+  }
+
+  // ---- fields: level 0 per mode, coarse levels sized by the largest hierarchy
+  {
+    for (int l = 0; l < s->lmax; l++) {
+      long Smax = 0;
+      for (int h = 0; h < 3; h++) Smax = std::max(Smax, s->hier[h][l].S);
+      const size_t n3 = (size_t)3 * Smax * s->nrhs;
+      if (!mixed || l == 0) {
+        // FP64 fields; in MIXED mode level 0 holds x (u64) and b*vol (f64)
+        TRY(s->alloc((void**)&s->u64[l], n3 * sizeof(double2)));
+        TRY(s->alloc((void**)&s->f64[l], n3 * sizeof(double2)));
+        if (!mixed) TRY(s->alloc((void**)&s->r64[l], n3 * sizeof(double2)));
+      }
+      if (mixed) {
+        TRY(s->alloc((void**)&s->u32[l], n3 * sizeof(float2)));
+        TRY(s->alloc((void**)&s->f32[l], n3 * sizeof(float2)));
+        TRY(s->alloc((void**)&s->r32[l], n3 * sizeof(float2)));
+      }
+    }
+    // line-sweep scratch: largest (level, direction) over the hierarchies,
+    // chunked over RHS so it stays below ~8 GB
+    long per_rhs = 0;
+    for (int h = 0; h < 3; h++)
+      for (int l = 0; l + 1 < s->lmax; l++)
+        for (int d = 0; d < 3; d++)
+          if (s->hier[h][l + 1].sc[d] == 2)
+            per_rhs = std::max(per_rhs, line_scratch_elems(s->hier[h][l].n, d, 1));
+    const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+    const size_t cap = (size_t)8 << 30;
+    s->chunk = s->nrhs;
+    while (s->chunk > 1 && (size_t)per_rhs * esz * s->chunk > cap) s->chunk = (s->chunk + 1) / 2;
+    s->scratch_bytes = std::max<size_t>((size_t)per_rhs * esz * s->chunk, 16);
+    TRY(s->alloc(&s->scratch, s->scratch_bytes));
+  }
+
+  // ---- graphs
+  if (s->opt.use_graphs) {
+    rc = mixed ? s->build_graphs<float>() : s->build_graphs<double>();
+    if (rc != EMMI_OK) {
+      emmi_solver_destroy(s);
+      return rc;
+    }
+  }
+  *out = s;
+  return EMMI_OK;
+#undef TRY
+#undef CKS
+}
+
+static int run_part(emmi_solver* s, int h, int part) {
+  if (s->opt.use_graphs) {
+    CK(cudaGraphLaunch(part ? s->gB[h] : s->gA[h], s->st));
+    s->last_launches += part ? s->nodesB[h] : s->nodesA[h];
+    return EMMI_OK;
+  }
+  const long before = s->launch_counter;
+  int cur = 0;
+  if (s->opt.precision == EMMI_PREC_MIXED)
+    s->emit_cycle<float>(h, 0, s->opt.cycleopt, part, cur);
+  else
+    s->emit_cycle<double>(h, 0, s->opt.cycleopt, part, cur);
+  s->last_launches += s->launch_counter - before;
+  CK(cudaGetLastError());
+  return EMMI_OK;
+}
+
+static int upload_mask(emmi_solver* s, int* dev, const std::vector<int>& host) {
+  CK(cudaMemcpyAsync(dev, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice, s->st));
+  return EMMI_OK;
+}
+
+static int read_norms(emmi_solver* s, const double* dev, std::vector<double>& host) {
+  CK(cudaMemcpyAsync(host.data(), dev, host.size() * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return EMMI_OK;
+}
+
+int emmi_solver_solve(emmi_solver* s, const double* b, double* x, double* h, int device,
+                      emmi_rhs_stats* stats) {
+  if (!s || !b || !x) {
+    set_err("emmi_solver_solve: null argument");
+    return EMMI_EINVAL;
+  }
+  const int nrhs = s->nrhs;
+  const long S = s->hier[0][0].S;
+  const long n3s = 3 * S;
+  const size_t fbytes = (size_t)n3s * nrhs * sizeof(double2);
+  const bool mixed = s->opt.precision == EMMI_PREC_MIXED;
+  int rc;
+  s->last_launches = 0;
+  CK(cudaEventRecord(s->ev0, s->st));
+  // b -> device (into u64[0] temporarily), then f64[0] = b * dual volume
+  double2* bdev = s->u64[0];
+  if (device)
+    CK(cudaMemcpyAsync(bdev, b, fbytes, cudaMemcpyDeviceToDevice, s->st));
+  else
+    CK(cudaMemcpyAsync(bdev, b, fbytes, cudaMemcpyHostToDevice, s->st));
+  {
+    dim3 g(blocks_for(S), nrhs);
+    k_scale_dual<<<g, 256, 0, s->st>>>(bdev, s->f64[0], s->geo64[0][0], s->d_op, s->gstride,
+                                       s->gmax1, s->n[0], s->n[1], s->n[2]);
+    s->last_launches++;
+  }
+  CK(cudaMemsetAsync(s->u64[0], 0, fbytes, s->st));  // x = 0 (gmg.c:1900)
+  std::vector<int>& act = s->h_active;
+  std::vector<int>& ref = s->h_refine;
+  act.assign(nrhs, 1);
+  ref.assign(nrhs, 0);
+  std::vector<double> nrm(nrhs), rnorm0(nrhs, 0.0), rn(nrhs, 0.0);
+  std::vector<int> cycles(nrhs, 0), status(nrhs, EMMI_SOLVE_MAXIT), nref(nrhs, 0),
+      since(nrhs, 0);
+  std::vector<double> best(nrhs, INFINITY);
+  std::vector<int> stall(nrhs, 0);
+  if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
+  const double tol = s->opt.tol;
+  const int ncycle = s->opt.ncycle;
+
+  if (mixed) {
+    // initial FP64 residual = b*vol (x = 0) -> f32[0]; rnorm0
+    LevelView<double> V64 = s->view<double>(0, 0);
+    V64.u = s->u64[0];
+    V64.f = s->f64[0];
+    V64.active = s->d_active;
+    CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
+    launch_residual<double, float>(V64, s->f32[0], s->d_norm64, s->st);
+    s->last_launches++;
+    launch_zero<float>(s->u32[0], n3s * nrhs, s->st);
+    s->last_launches++;
+    if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
+    for (int r = 0; r < nrhs; r++) {
+      rnorm0[r] = std::sqrt(nrm[r]);
+      rn[r] = rnorm0[r];
+      if (!(rnorm0[r] > 0) || !std::isfinite(rnorm0[r])) {
+        act[r] = 0;
+        status[r] = std::isfinite(rnorm0[r]) ? EMMI_SOLVE_OK : EMMI_SOLVE_NONFINITE;
+      }
+    }
+    if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
+    for (int icycle = 0; icycle < ncycle; icycle++) {
+      bool any = false;
+      for (int r = 0; r < nrhs; r++) any |= act[r] != 0;
+      if (!any) break;
+      const int hh = s->opt.isemicoarsen ? icycle % 3 : 0;
+      if ((rc = run_part(s, hh, 0)) != EMMI_OK) return rc;
+      if (s->has_norm) {
+        if ((rc = read_norms(s, s->d_norm, nrm)) != EMMI_OK) return rc;
+        // complex64 estimate of |b - A(x+u)|; refine when it says converged
+        // or every refine_every cycles
+        bool anyref = false;
+        for (int r = 0; r < nrhs; r++) {
+          ref[r] = 0;
+          if (!act[r]) continue;
+          const double est = std::sqrt(nrm[r]) / rnorm0[r];
+          if (s->opt.verb) printf("icycle=%d rnorm=%e\n", icycle, est * rnorm0[r]);
+          if ((est < tol && since[r] > 0) || since[r] >= s->opt.refine_every || !std::isfinite(est)) {
+            ref[r] = 1;
+            anyref = true;
+          }
+        }
+        if (anyref) {
+          if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
+          dim3 g(blocks_for(n3s, 256, 2048), nrhs);
+          k_accumulate<<<g, 256, 0, s->st>>>(s->u64[0], s->u32[0], n3s, s->d_refine);
+          LevelView<double> W = s->view<double>(0, 0);
+          W.u = s->u64[0];
+          W.f = s->f64[0];
+          W.active = s->d_refine;
+          CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
+          launch_residual<double, float>(W, s->f32[0], s->d_norm64, s->st);
+          k_zero_masked<<<g, 256, 0, s->st>>>(s->u32[0], n3s, s->d_refine);
+          s->last_launches += 3;
+          if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
+          for (int r = 0; r < nrhs; r++) {
+            if (!ref[r]) continue;
+            nref[r]++;
+            since[r] = 0;
+            rn[r] = std::sqrt(nrm[r]);
+            const double rel = rn[r] / rnorm0[r];
+            if (!std::isfinite(rel)) {
+              act[r] = 0;
+              status[r] = EMMI_SOLVE_NONFINITE;
+            } else if (rel <= tol) {
+              act[r] = 0;
+              status[r] = EMMI_SOLVE_OK;
+            } else {
+              if (rel < 0.5 * best[r]) {
+                best[r] = rel;
+                stall[r] = 0;
+              } else if (++stall[r] >= 4) {
+                act[r] = 0;
+                status[r] = EMMI_SOLVE_STALL;
+              }
+            }
+          }
+          if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
+          // the new inner problem starts from u = 0: its level-0 residual
+          // (what part B restricts) is f; recompute it for the refined RHS
+          for (int r = 0; r < nrhs; r++) ref[r] = ref[r] && act[r];
+          if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
+          LevelView<float> R = s->view<float>(hh, 0);
+          R.active = s->d_refine;
+          launch_residual<float, float>(R, R.r, nullptr, s->st);
+          s->last_launches++;
+        }
+      }
+      if ((rc = run_part(s, hh, 1)) != EMMI_OK) return rc;
+      for (int r = 0; r < nrhs; r++)
+        if (act[r]) {
+          cycles[r]++;
+          since[r]++;
+        }
+    }
+    // RHS still cycling at ncycle: fold in the last correction and measure
+    bool anyleft = false;
+    for (int r = 0; r < nrhs; r++) {
+      ref[r] = act[r];
+      anyleft |= act[r] != 0;
+    }
+    if (anyleft) {
+      if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
+      dim3 g(blocks_for(n3s, 256, 2048), nrhs);
+      k_accumulate<<<g, 256, 0, s->st>>>(s->u64[0], s->u32[0], n3s, s->d_refine);
+      LevelView<double> W = s->view<double>(0, 0);
+      W.u = s->u64[0];
+      W.f = s->f64[0];
+      W.active = s->d_refine;
+      CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
+      launch_residual<double, float>(W, s->f32[0], s->d_norm64, s->st);
+      s->last_launches += 2;
+      if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
+      for (int r = 0; r < nrhs; r++)
+        if (ref[r]) {
+          nref[r]++;
+          rn[r] = std::sqrt(nrm[r]);
+          status[r] = rn[r] / rnorm0[r] <= tol ? EMMI_SOLVE_OK
+                      : std::isfinite(rn[r]) ? EMMI_SOLVE_MAXIT : EMMI_SOLVE_NONFINITE;
+        }
+    }
+  } else {
+    // plain FP64 cycles on u64/f64 (gmg_apply, gmg.c:1911-1926)
+    for (int icycle = 0; icycle < ncycle; icycle++) {
+      bool any = false;
+      for (int r = 0; r < nrhs; r++) any |= act[r] != 0;
+      if (!any) break;
+      const int hh = s->opt.isemicoarsen ? icycle % 3 : 0;
+      if ((rc = run_part(s, hh, 0)) != EMMI_OK) return rc;
+      if (s->has_norm) {
+        if ((rc = read_norms(s, s->d_norm, nrm)) != EMMI_OK) return rc;
+        bool changed = false;
+        for (int r = 0; r < nrhs; r++) {
+          if (!act[r]) continue;
+          const double rnorm = std::sqrt(nrm[r]);
+          if (s->opt.verb) printf("icycle=%d rnorm=%e\n", icycle, rnorm);
+          rn[r] = rnorm;
+          if (icycle == 0) {
+            rnorm0[r] = rnorm;
+            if (!(rnorm > 0)) {
+              act[r] = 0;
+              status[r] = std::isfinite(rnorm) ? EMMI_SOLVE_OK : EMMI_SOLVE_NONFINITE;
+              changed = true;
+            }
+          } else if (!std::isfinite(rnorm)) {
+            act[r] = 0;
+            status[r] = EMMI_SOLVE_NONFINITE;
+            changed = true;
+          } else if (rnorm < rnorm0[r] * tol) {
+            act[r] = 0;
+            status[r] = EMMI_SOLVE_OK;
+            changed = true;
+          }
+        }
+        if (changed && (rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
+      }
+      if ((rc = run_part(s, hh, 1)) != EMMI_OK) return rc;
+      for (int r = 0; r < nrhs; r++)
+        if (act[r]) cycles[r]++;
+    }
+    // final FP64 residual of every RHS for the statistics
+    act.assign(nrhs, 1);
+    if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
+    LevelView<double> V = s->view<double>(0, 0);
+    CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
+    launch_residual<double, double>(V, V.r, s->d_norm64, s->st);
+    s->last_launches++;
+    if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
+    for (int r = 0; r < nrhs; r++) {
+      rn[r] = std::sqrt(nrm[r]);
+      if (status[r] == EMMI_SOLVE_MAXIT && !std::isfinite(rn[r])) status[r] = EMMI_SOLVE_NONFINITE;
+    }
+  }
+  // outputs: x = E, h = curl E / (i w mu0) (gmg.c:1927-1929)
+  if (device)
+    CK(cudaMemcpyAsync(x, s->u64[0], fbytes, cudaMemcpyDeviceToDevice, s->st));
+  else
+    CK(cudaMemcpyAsync(x, s->u64[0], fbytes, cudaMemcpyDeviceToHost, s->st));
+  if (h) {
+    // H goes to f64[0] (b*vol is no longer needed) then out
+    dim3 g(blocks_for(S), nrhs);
+    k_curl_h<<<g, 256, 0, s->st>>>(s->u64[0], s->f64[0], s->geo64[0][0], s->d_op, s->d_wmu64,
+                                   s->gstride, s->gmax1, s->n[0], s->n[1], s->n[2]);
+    s->last_launches++;
+    if (device)
+      CK(cudaMemcpyAsync(h, s->f64[0], fbytes, cudaMemcpyDeviceToDevice, s->st));
+    else
+      CK(cudaMemcpyAsync(h, s->f64[0], fbytes, cudaMemcpyDeviceToHost, s->st));
+  }
+  CK(cudaEventRecord(s->ev1, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaGetLastError());
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  s->last_time = ms * 1e-3;
+  if (stats)
+    for (int r = 0; r < nrhs; r++) {
+      stats[r].cycles = cycles[r];
+      stats[r].status = status[r];
+      stats[r].rnorm0 = rnorm0[r];
+      stats[r].rnorm = rn[r];
+      stats[r].refinements = nref[r];
+    }
+  return EMMI_OK;
+}
+
+double emmi_solver_last_time(const emmi_solver* s) { return s ? s->last_time : 0.0; }
+long emmi_solver_last_launches(const emmi_solver* s) { return s ? s->last_launches : 0; }
+size_t emmi_solver_device_bytes(const emmi_solver* s) { return s ? s->bytes : 0; }
+
+void emmi_solver_destroy(emmi_solver* s) {
+  if (!s) return;
+  if (s->st) cudaStreamSynchronize(s->st);
+  for (int h = 0; h < 3; h++) {
+    if (s->gA[h]) cudaGraphExecDestroy(s->gA[h]);
+    if (s->gB[h]) cudaGraphExecDestroy(s->gB[h]);
+  }
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ single level
+namespace {
+struct OneLevel {
+  std::vector<void*> ptrs;
+  ~OneLevel() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename P> cudaError_t get(P** p, size_t b) {
+    cudaError_t e = cudaMalloc((void**)p, b);
+    if (e == cudaSuccess) ptrs.push_back(*p);
+    return e;
+  }
+};
+
+template <typename T>
+int level_op(const int n[3], const double* x1, const double* x2, const double* x3,
+             const double* cells, double omega, int dir, int iter, double* u, const double* f,
+             double* r, double* norm) {
+  OneLevel M;
+  const int gmax = std::max(n[0], std::max(n[1], n[2]));
+  const int gmax1 = gmax + 1, gstride = 9 * gmax1;
+  std::vector<double> g(gstride, 0.0), xs(gmax1);
+  const double* xin[3] = {x1, x2, x3};
+  for (int e = 0; e < 3; e++) {
+    for (int i = 0; i <= n[e]; i++) g[e * gmax1 + i] = xin[e][i];
+    stagger(n[e], g.data() + e * gmax1, xs.data(), g.data() + (6 + e) * gmax1,
+            g.data() + (3 + e) * gmax1);
+  }
+  std::vector<T> gT(gstride);
+  for (int i = 0; i < gstride; i++) gT[i] = (T)g[i];
+  const long S = (long)(n[0] + 1) * (n[1] + 1) * (n[2] + 1);
+  const long nc = (long)n[0] * n[1] * n[2];
+  std::vector<T> cT(4 * nc);
+  for (long i = 0; i < 4 * nc; i++) cT[i] = (T)cells[i];
+  std::vector<C_t<T>> uT(3 * S), fT(3 * S);
+  for (long i = 0; i < 3 * S; i++) {
+    uT[i] = mk<T>((T)u[2 * i], (T)u[2 * i + 1]);
+    fT[i] = mk<T>((T)f[2 * i], (T)f[2 * i + 1]);
+  }
+  LevelView<T> V;
+  for (int e = 0; e < 3; e++) V.n[e] = n[e];
+  V.nrhs = 1;
+  V.S = S;
+  V.ncell = nc;
+  V.gstride = gstride;
+  V.gmax1 = gmax1;
+  T* dg;
+  T* dc;
+  T* dw;
+  C_t<T>*du, *df, *dr;
+  double* dn;
+  void* scr = nullptr;
+  const T wmu = (T)(omega * kMu0);
+  CK(M.get(&dg, gstride * sizeof(T)));
+  CK(M.get(&dc, 4 * nc * sizeof(T)));
+  CK(M.get(&dw, sizeof(T)));
+  CK(M.get(&du, 3 * S * sizeof(C_t<T>)));
+  CK(M.get(&df, 3 * S * sizeof(C_t<T>)));
+  CK(M.get(&dr, 3 * S * sizeof(C_t<T>)));
+  CK(M.get(&dn, sizeof(double)));
+  CK(cudaMemcpy(dg, gT.data(), gstride * sizeof(T), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dc, cT.data(), 4 * nc * sizeof(T), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dw, &wmu, sizeof(T), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(du, uT.data(), 3 * S * sizeof(C_t<T>), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(df, fT.data(), 3 * S * sizeof(C_t<T>), cudaMemcpyHostToDevice));
+  CK(cudaMemset(dn, 0, sizeof(double)));
+  V.geo = dg;
+  V.cells = dc;
+  V.u = du;
+  V.f = df;
+  V.r = dr;
+  V.wmu = dw;
+  V.active = nullptr;
+  V.op = nullptr;
+  if (r) {
+    launch_residual<T, T>(V, dr, dn, 0);
+  } else if (dir < 3) {
+    CK(M.get((C_t<T>**)&scr, line_scratch_elems(n, dir, 1) * sizeof(C_t<T>) + 16));
+    for (int cc = 0; cc < 4; cc++)
+      launch_line_sweep<T>(V, dir, iter % 2 ? 3 - cc : cc, (C_t<T>*)scr, 0);
+  } else {
+    for (int cc = 0; cc < 8; cc++) launch_point_sweep<T>(V, iter % 2 ? 7 - cc : cc, 0);
+  }
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  std::vector<C_t<T>> out(3 * S);
+  CK(cudaMemcpy(out.data(), r ? dr : du, 3 * S * sizeof(C_t<T>), cudaMemcpyDeviceToHost));
+  double* dst = r ? r : u;
+  for (long i = 0; i < 3 * S; i++) {
+    dst[2 * i] = (double)out[i].x;
+    dst[2 * i + 1] = (double)out[i].y;
+  }
+  if (norm) {
+    double nn;
+    CK(cudaMemcpy(&nn, dn, sizeof(double), cudaMemcpyDeviceToHost));
+    *norm = std::sqrt(nn);
+  }
+  return EMMI_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int emmi_level_residual(const int n[3], const double* x1, const double* x2, const double* x3,
+                        const double* cells, double omega, int prec, const double* u,
+                        const double* f, double* r, double* norm) {
+  if (!n || !x1 || !x2 || !x3 || !cells || !u || !f || !r) {
+    set_err("emmi_level_residual: null argument");
+    return EMMI_EINVAL;
+  }
+  double* uc = const_cast<double*>(u);
+  return prec == EMMI_PREC_FP64
+             ? level_op<double>(n, x1, x2, x3, cells, omega, 0, 0, uc, f, r, norm)
+             : level_op<float>(n, x1, x2, x3, cells, omega, 0, 0, uc, f, r, norm);
+}
+
+int emmi_level_smooth(const int n[3], const double* x1, const double* x2, const double* x3,
+                      const double* cells, double omega, int prec, int dir, int iter, double* u,
+                      const double* f) {
+  if (!n || !x1 || !x2 || !x3 || !cells || !u || !f || dir < 0 || dir > 3) {
+    set_err("emmi_level_smooth: bad argument");
+    return EMMI_EINVAL;
+  }
+  return prec == EMMI_PREC_FP64
+             ? level_op<double>(n, x1, x2, x3, cells, omega, dir, iter, u, f, nullptr, nullptr)
+             : level_op<float>(n, x1, x2, x3, cells, omega, dir, iter, u, f, nullptr, nullptr);
+}
+
+}  // extern "C"
+

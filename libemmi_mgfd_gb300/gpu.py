@@ -1,0 +1,205 @@
+"""ctypes front of libemmi_gpu.so: the batched GB300 solver and the
+single-level operators.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+present, these calls raise.  Arrays follow the reference layout: fields are
+complex128 of length 3*(n1+1)*(n2+1)*(n3+1) per right-hand side
+(component-major, i fastest); cells are float32 [4][n3][n2][n1]
+(sigma11, sigma22, sigma33, invmur).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GPU_LIB = os.path.join(HERE, "libemmi_gpu.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+STATUS = {0: "ok", 1: "maxit", 2: "stall", 3: "nonfinite"}
+
+_lib = None
+
+
+class EmmiError(RuntimeError):
+    pass
+
+
+class _Problem(C.Structure):
+    _fields_ = [("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int), ("nop", C.c_int),
+                ("nrhs", C.c_int), ("x1", C.c_void_p), ("x2", C.c_void_p), ("x3", C.c_void_p),
+                ("cells", C.c_void_p), ("op", C.c_void_p), ("omega", C.c_void_p)]
+
+
+class _Options(C.Structure):
+    _fields_ = [("cycleopt", C.c_int), ("ncycle", C.c_int), ("v1", C.c_int), ("v2", C.c_int),
+                ("tol", C.c_double), ("isemicoarsen", C.c_int), ("precision", C.c_int),
+                ("sigma_floor", C.c_double), ("refine_every", C.c_int),
+                ("use_graphs", C.c_int), ("verb", C.c_int)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("cycles", C.c_int), ("status", C.c_int), ("rnorm0", C.c_double),
+                ("rnorm", C.c_double), ("refinements", C.c_int)]
+
+
+def lib():
+    """Load libemmi_gpu.so (built by libemmi_mgfd_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(GPU_LIB):
+            raise EmmiError(f"{GPU_LIB} is missing: run libemmi_mgfd_gb300.build.build()")
+        L = C.CDLL(GPU_LIB)
+        L.emmi_last_error.restype = C.c_char_p
+        L.emmi_solver_last_time.restype = C.c_double
+        L.emmi_solver_last_launches.restype = C.c_long
+        L.emmi_solver_device_bytes.restype = C.c_size_t
+        L.emmi_solver_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(_Problem),
+                                         C.POINTER(_Options)]
+        L.emmi_solver_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                        C.c_void_p]
+        L.emmi_solver_last_time.argtypes = [C.c_void_p]
+        L.emmi_solver_last_launches.argtypes = [C.c_void_p]
+        L.emmi_solver_device_bytes.argtypes = [C.c_void_p]
+        L.emmi_solver_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise EmmiError(f"{what} failed ({rc}): {lib().emmi_last_error().decode()}")
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class Options:
+    cycleopt: int = 2
+    ncycle: int = 30
+    v1: int = 1
+    v2: int = 1
+    tol: float = 1e-6
+    isemicoarsen: int = 1
+    precision: int = PREC_MIXED
+    sigma_floor: float = 0.0
+    refine_every: int = 3
+    use_graphs: int = 1
+    verb: int = 0
+
+    def _c(self) -> _Options:
+        return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
+                        self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
+                        self.verb)
+
+
+class Solver:
+    """A batch of right-hand sides over one or more operators.
+
+    x1,x2,x3: float32 [nop, n+1] node coordinates; cells: float32
+    [nop, 4, n3, n2, n1]; omega: float32 [nrhs]; op: int [nrhs] or None."""
+
+    def __init__(self, n: Sequence[int], x1, x2, x3, cells, omega, op=None,
+                 options: Optional[Options] = None):
+        self.n = tuple(int(v) for v in n)
+        self.x1 = np.ascontiguousarray(np.atleast_2d(x1), np.float32)
+        self.x2 = np.ascontiguousarray(np.atleast_2d(x2), np.float32)
+        self.x3 = np.ascontiguousarray(np.atleast_2d(x3), np.float32)
+        self.cells = np.ascontiguousarray(cells, np.float32).reshape(self.x1.shape[0], 4, -1)
+        self.omega = np.ascontiguousarray(np.atleast_1d(omega), np.float32)
+        self.nop = self.x1.shape[0]
+        self.nrhs = self.omega.shape[0]
+        self.op = None if op is None else np.ascontiguousarray(op, np.int32)
+        self.options = options or Options()
+        n1, n2, n3 = self.n
+        self.nslots = (n1 + 1) * (n2 + 1) * (n3 + 1)
+        prob = _Problem(n1, n2, n3, self.nop, self.nrhs, _p(self.x1).value, _p(self.x2).value,
+                        _p(self.x3).value, _p(self.cells).value,
+                        None if self.op is None else _p(self.op).value, _p(self.omega).value)
+        h = C.c_void_p()
+        _check(lib().emmi_solver_create(C.byref(h), C.byref(prob), C.byref(self.options._c())),
+               "emmi_solver_create")
+        self._h = h
+
+    def solve(self, b, want_h: bool = True, device: bool = False, x_out=None, h_out=None):
+        """Solve for every RHS.  Host mode: b complex128 [nrhs, 3S] numpy ->
+        returns (x, h, stats).  Device mode: b, x_out, h_out are integer
+        device pointers (e.g. torch .data_ptr()) -> returns stats."""
+        st = (_Stats * self.nrhs)()
+        if device:
+            _check(lib().emmi_solver_solve(self._h, C.c_void_p(b), C.c_void_p(x_out),
+                                           C.c_void_p(h_out) if h_out else None, 1, st),
+                   "emmi_solver_solve")
+            return self._stats(st)
+        b = np.ascontiguousarray(b, np.complex128).reshape(self.nrhs, 3 * self.nslots)
+        x = np.zeros_like(b)
+        h = np.zeros_like(b) if want_h else None
+        _check(lib().emmi_solver_solve(self._h, _p(b), _p(x), _p(h) if want_h else None, 0, st),
+               "emmi_solver_solve")
+        return x, h, self._stats(st)
+
+    @staticmethod
+    def _stats(st):
+        return [dict(cycles=s.cycles, status=STATUS.get(s.status, s.status), rnorm0=s.rnorm0,
+                     rnorm=s.rnorm, rel=(s.rnorm / s.rnorm0 if s.rnorm0 > 0 else 0.0),
+                     refinements=s.refinements) for s in st]
+
+    @property
+    def last_time(self) -> float:
+        return lib().emmi_solver_last_time(self._h)
+
+    @property
+    def last_launches(self) -> int:
+        return lib().emmi_solver_last_launches(self._h)
+
+    @property
+    def device_bytes(self) -> int:
+        return lib().emmi_solver_device_bytes(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().emmi_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _level_args(n, x, cells):
+    n3 = (C.c_int * 3)(*[int(v) for v in n])
+    xs = [np.ascontiguousarray(v, np.float64) for v in x]
+    c = np.ascontiguousarray(cells, np.float64)
+    return n3, xs, c
+
+
+def level_residual(n, x, cells, omega, u, f, prec=PREC_FP64):
+    """r = f - A u on one level (cells volume-weighted, float64 [4, ncell])."""
+    n3, xs, c = _level_args(n, x, cells)
+    u = np.ascontiguousarray(u, np.complex128)
+    f = np.ascontiguousarray(f, np.complex128)
+    r = np.zeros_like(u)
+    nrm = C.c_double()
+    _check(lib().emmi_level_residual(n3, _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(c), C.c_double(omega),
+                                     prec, _p(u), _p(f), _p(r), C.byref(nrm)), "emmi_level_residual")
+    return r, nrm.value
+
+
+def level_smooth(n, x, cells, omega, u, f, direction, prec=PREC_FP64, iter=0):
+    """One multicolour sweep: direction 0..2 lines along x/y/z, 3 node patches."""
+    n3, xs, c = _level_args(n, x, cells)
+    u = np.ascontiguousarray(u, np.complex128).copy()
+    f = np.ascontiguousarray(f, np.complex128)
+    _check(lib().emmi_level_smooth(n3, _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(c), C.c_double(omega),
+                                   prec, int(direction), int(iter), _p(u), _p(f)),
+           "emmi_level_smooth")
+    return u

@@ -1,0 +1,123 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_dump (the reference compiled from its own C sources by
+``make -C oracle ref``) on small seeded cases and stores what it wrote --
+grids, homogenized conductivities, injected right-hand sides, converged E/H
+slot fields, receiver data, volume extractions, adjoint sources and the
+mode=2 gradient -- as compressed .npz files.  The reference does not exist on
+GPU machines; these fixtures carry its outputs there.
+
+    python tests/golden/make_golden.py          (needs oracle/_ref built)
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from libemmi_mgfd_gb300 import workloads as W  # noqa: E402
+
+REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+
+
+def run_ref(s: W.Survey, extra, adjoint: int):
+    d = tempfile.mkdtemp(prefix="golden_")
+    s.write(d)
+    args = [REF_DUMP] + s.params(d) + [f"dumpdir={d}", f"adjoint={adjoint}", "verb=1"] + list(extra)
+    r = subprocess.run(args, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout + r.stderr)
+    return d, r.stdout
+
+
+def load(d, nm, dt):
+    return np.fromfile(os.path.join(d, nm), dt)
+
+
+def case(s: W.Survey, extra, adjoint=0, keep_fields=True, nfreq=1, tag=None):
+    d, out = run_ref(s, extra, adjoint)
+    f32, c128, c64 = np.float32, np.complex128, np.complex64
+    rec = {
+        "name": np.array(tag or s.name),
+        "params": np.array(" ".join(extra)),
+        "n": np.array(s.n, np.int32),
+        "nxyz": np.array([s.nx, s.ny, s.nz], np.int32),
+        "o": np.array([s.ox, s.oy, s.oz], f32),
+        "dxyz": np.array([s.dx, s.dy, s.dz], f32),
+        "rho11": s.rho11, "rho22": s.rho22, "rho33": s.rho33,
+        "sources": s.sources.astype(f32), "receivers": s.receivers.astype(f32),
+        "chsrc": np.array(",".join(s.chsrc)), "chrec": np.array(",".join(s.chrec)),
+        "freqs": np.array(s.freqs, f32),
+        "extra_keys": np.array(" ".join(f"{k}={v}" for k, v in s.extra.items())),
+        "omegas": load(d, "omegas", f32), "rho_water": load(d, "rho_water", f32),
+        "srcrec": load(d, "srcrec", f32), "dcal": load(d, "dcal", c64),
+    }
+    # residual history of each solve, as the reference prints it (gmg.c:1627)
+    solves, cur = [], None
+    for line in out.splitlines():
+        if "gmg_init" in line:
+            cur = []
+            solves.append(cur)
+        elif line.startswith("icycle=") and cur is not None:
+            cur.append(float(line.split("rnorm=")[1]))
+    rec["rnorm_fwd"] = np.array(solves[0] if solves else [], np.float64)
+    if adjoint and len(solves) > nfreq:
+        rec["rnorm_adj"] = np.array(solves[nfreq], np.float64)
+    for nm in ("x1", "x2", "x3", "x1s", "x2s", "x3s", "d1", "d2", "d3", "d1s", "d2s", "d3s",
+               "sigma11", "sigma22", "sigma33", "invmur"):
+        rec[nm] = load(d, nm, f32)
+    if keep_fields:
+        for f in range(nfreq):
+            for nm in (f"b_f{f}", f"x_f{f}", f"h_f{f}"):
+                rec[nm] = load(d, nm, c128)
+        for nm in ("E1", "E2", "E3", "H1", "H2", "H3"):
+            rec[nm] = load(d, nm, c64)
+    if adjoint:
+        rec["dres"] = load(d, "dres", c64)
+        for f in range(nfreq):
+            for nm in (f"badj_f{f}", f"madj_f{f}", f"xa_f{f}"):
+                rec[nm] = load(d, nm, c128)
+        for nm in ("E1a", "E2a", "E3a"):
+            rec[nm] = load(d, nm, c64)
+        rec["grad"] = load(d, "grad", f32)
+        rec["phess"] = load(d, "phess", f32)
+        rec["bathy"] = np.array(1000.0, f32)
+    return rec
+
+
+def main():
+    if not os.path.exists(REF_DUMP):
+        sys.exit("oracle/_ref/ref_dump missing: run `make -C oracle ref` first")
+    out = {}
+    # 1. tiny layered, F-cycles: converged fields + mode=2 adjoint/gradient
+    out["tiny_layered"] = case(W.tiny_layered(), ["tol=1e-10", "ncycle=60"], adjoint=1)
+    # 2. the same after exactly 3 cycles (iterate-level pin of the oracle)
+    out["tiny_layered_it3"] = case(W.tiny_layered(), ["tol=0", "ncycle=3"], tag="tiny_layered_it3")
+    # 3. anisotropic, rotated/tilted source, all channels, non-cubic mesh
+    out["tiny_aniso"] = case(W.tiny_aniso(n=(16, 8, 16)), ["tol=1e-10", "ncycle=80"])
+    # 4. V-cycle / W-cycle / no semi-coarsening iterates
+    out["tiny_vcycle_it3"] = case(W.tiny_layered(), ["tol=0", "ncycle=3", "cycleopt=1"],
+                                  tag="tiny_vcycle_it3")
+    out["tiny_wcycle_it2"] = case(W.tiny_layered(), ["tol=0", "ncycle=2", "cycleopt=3"],
+                                  tag="tiny_wcycle_it2")
+    out["tiny_point_it3"] = case(W.tiny_layered(), ["tol=0", "ncycle=3", "isemicoarsen=0"],
+                                 tag="tiny_point_it3")
+    # 5. the reference's own CPU-runnable configuration (64^3), receivers only
+    out["c1_layered_64"] = case(W.config1(64), ["tol=1e-8", "ncycle=60"], keep_fields=False,
+                                tag="c1_layered_64")
+    for k, rec in out.items():
+        if k == "c1_layered_64":
+            # keep the fixture small: conductivities are layered, compress well
+            pass
+        np.savez_compressed(os.path.join(HERE, f"{k}.npz"), **rec)
+        print(k, os.path.getsize(os.path.join(HERE, f"{k}.npz")) // 1024, "KB")
+
+
+if __name__ == "__main__":
+    main()
