@@ -1,0 +1,420 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 hot path: solves/s to 1e-8 relative residual at
+128^3, mixed-precision GMG against plain FP64 GMG.
+
+Workload (one step): the mixed-precision 128^3 configuration -- 25 shots on
+a 5x5 grid at 1 km over a log-normal sediment under 1000 m of water with two
+resistive bodies, 1 Hz, 100 seafloor receivers, Ex source, Ex/Ey/Hx/Hy
+channels -- as one batch: inject the 25 sources, solve all 25 systems to
+|b - A x| <= 1e-8 |b| (FP64 residual), extract the receiver data.
+
+  value  solves/s with the operators and right-hand sides resident in HBM
+  e2e    the same through the C ABI from host arrays: solver setup (H2D of
+         the 25 meshes and conductivity cubes), inject, solve, extract, D2H
+         of the receiver data
+  plain_fp64   the same batch with complex128 cycles (the reference's
+         arithmetic), for the mixed-vs-plain ratio
+  roofline     the level-0 line-relaxation sweep (dominant kernel), timed
+         live with CUDA events on the solver's stream
+  cpu_baseline the CPU restatement of the reference's algorithm on the host
+         cores, one F-cycle per thread as a bounded sample, scaled by the
+         cycles a solve takes
+
+  python bench.py [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank solves its own copy of the batch (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s to 1e-8 rel. residual at 128³ on 1 GB300: learned+mixed vs plain GMG"
+UNIT = "solves/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=128)
+    p.add_argument("--tol", type=float, default=1e-8)
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--nrhs", type=int, default=0, help="use only the first k shots")
+    p.add_argument("--profile", action="store_true",
+                   help="one shot: a short solve, then one level-0 line sweep inside the NVTX "
+                        "range emmi_profile (for ncu --nvtx-include emmi_profile/)")
+    return p.parse_args()
+
+
+def dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as D
+        D.init_process_group("gloo")
+        pg = D
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)])
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- workload
+def build_workload(n: int):
+    """25 shots of the 128^3 configuration through the C host front end."""
+    from libemmi_mgfd_gb300 import host
+    from libemmi_mgfd_gb300 import workloads as W
+    s = W.config3(n)
+    m = host.Model.from_survey(s)
+    src = s.sources.astype(np.float32)
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        grids = list(ex.map(lambda p: m.regrid(float(p[0]), float(p[1]), float(p[2])), src))
+    X1 = np.stack([g["x1"] for g in grids])
+    X2 = np.stack([g["x2"] for g in grids])
+    X3 = np.stack([g["x3"] for g in grids])
+    cells = np.stack([np.stack([g["sigma11"], g["sigma22"], g["sigma33"], g["invmur"]])
+                      for g in grids])
+    om = np.float32(2.0 * np.pi * s.freqs[0])
+    srcr = src.copy()
+    srcr[:, 3:] = np.deg2rad(srcr[:, 3:])
+    rec = s.receivers.astype(np.float32).copy()
+    rec[:, 3:] = np.deg2rad(rec[:, 3:])
+    return dict(survey=s, X1=X1, X2=X2, X3=X3, cells=cells, omega=np.full(len(src), om, np.float32),
+                rho_water=np.float32(m.rho_water()), src=srcr, rec=rec, grids=grids)
+
+
+def make_solver(w, precision, tol):
+    from libemmi_mgfd_gb300 import gpu as G
+    n = w["survey"].n
+    nrhs = w["X1"].shape[0]
+    return G.Solver(n, w["X1"], w["X2"], w["X3"], w["cells"], w["omega"],
+                    op=np.arange(nrhs, dtype=np.int32),
+                    options=G.Options(precision=precision, tol=tol, ncycle=100),
+                    rho_water=w["rho_water"])
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per line-sweep launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "line_sweep_c3_128.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_scaled="):
+                return float(line.split("=")[1])
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------- CPU leg
+def cpu_sample(w, nthreads, cycles_per_solve, ncyc=1):
+    """Oracle (the reference's algorithm, lexicographic sweeps) on host
+    threads: each thread one shot, `ncyc` F-cycles including its setup.
+    Returns (solves/s, seconds, sample text)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    s = w["survey"]
+    n = s.n
+    nshots = w["X1"].shape[0]
+    from libemmi_mgfd_gb300 import workloads as W  # noqa: F401
+    # right-hand sides by the oracle's restatement of inject_source
+    grids = w["grids"]
+    bs = []
+    for i in range(nthreads):
+        g = grids[i % nshots]
+        G = O.Grid(n, g["x1"], g["x2"], g["x3"], g["x1s"], g["x2s"], g["x3s"], g["d1"], g["d2"],
+                   g["d3"], g["sigma33"], float(w["rho_water"]))
+        bs.append(O.inject_source(G, w["src"][i % nshots], s.chsrc, float(w["omega"][0])))
+
+    def one(i):
+        g = grids[i % nshots]
+        O.gmg_solve(n, g["x1"], g["x2"], g["x3"], g["sigma11"], g["sigma22"], g["sigma33"],
+                    g["invmur"], float(w["omega"][0]), bs[i], ncycle=ncyc, tol=0.0,
+                    ordering=O.ORDER_LEX)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
+        list(ex.map(one, range(nthreads)))
+    dt = time.perf_counter() - t0
+    value = nthreads * ncyc / (dt * cycles_per_solve)
+    sample = (f"{nthreads} concurrent shots x {ncyc} F-cycle(s) of the {n[0]}^3 system "
+              f"(setup included) in {dt:.1f} s, scaled by {cycles_per_solve:.1f} cycles per solve")
+    return value, dt, sample
+
+
+# ---------------------------------------------------------------- main
+def main():
+    a = parse()
+    rank, world, local, pg = dist()
+    if a.impl == "reference":
+        return reference_arm(a, rank, world, pg)
+    import torch
+    from libemmi_mgfd_gb300 import build as B
+    from libemmi_mgfd_gb300 import gpu as G
+    B.build()
+    torch.cuda.set_device(local)
+    w = build_workload(a.n)
+    s = w["survey"]
+    if a.nrhs > 0 or a.profile:
+        k = 1 if a.profile else a.nrhs
+        for key in ("X1", "X2", "X3", "cells", "omega", "src"):
+            w[key] = np.ascontiguousarray(w[key][:k])
+        w["grids"] = w["grids"][:k]
+    nrhs = w["X1"].shape[0]
+    if a.profile:
+        sp = make_solver(w, G.PREC_MIXED, a.tol)
+        sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+        torch.cuda.nvtx.range_push("emmi_profile")
+        sp.time_smoother(0, reps=1)
+        torch.cuda.nvtx.range_pop()
+        sp.close()
+        print(json.dumps({"profile": "done", "n": a.n, "nrhs": nrhs}))
+        return
+
+    solver = make_solver(w, G.PREC_MIXED, a.tol)
+    ext = torch.cuda.ExternalStream(solver.stream)
+    launches = []
+    stats = None
+
+    def step():
+        d, st, _ = solver.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+        launches.append(solver.last_launches + 2)  # + injection + extraction
+        return d, st
+
+    for _ in range(a.warmup):
+        step()
+    barrier(pg)
+    torch.cuda.synchronize()
+    times = []
+    launches.clear()
+    with ClockSampler(local) as clk:
+        for _ in range(a.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            d, stats = step()
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize()
+    barrier(pg)
+    total = max_over_ranks(pg, sum(times))
+    value = nrhs * a.steps * world / total
+    cycles = [x["cycles"] for x in stats]
+    rels = [x["rel"] for x in stats]
+    refs = [x["refinements"] for x in stats]
+    ok = all(x["status"] == "ok" for x in stats)
+
+    # roofline of the dominant kernel (level-0 line relaxation)
+    ms, nl, by = solver.time_smoother(0, reps=5)
+    peak, peak_kind = peaks()
+    achieved = by / (ms * 1e-3) / 1e9
+    traffic = ncu_traffic()
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "kernel": "k_line_sweep<float,0> (level 0, 4 colours, 25 RHS)",
+            "ms_per_sweep": round(ms, 4), "launches_per_sweep": nl,
+            "algorithmic_bytes_per_launch": by / nl, "peak_kind": peak_kind}
+    solver.close()
+
+    # e2e: from host arrays through the C ABI, solver setup included
+    e2e_times, h2d, d2h = [], 0, 0
+    for it in range(0 if a.no_e2e else 2):
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        sv = make_solver(w, G.PREC_MIXED, a.tol)
+        _, _, (hb, db) = sv.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+        sv.close()
+        t1.record()
+        t1.synchronize()
+        if it > 0:
+            e2e_times.append(t0.elapsed_time(t1) / 1e3)
+        h2d = (w["X1"].nbytes + w["X2"].nbytes + w["X3"].nbytes + w["cells"].nbytes
+               + w["omega"].nbytes + hb)
+        d2h = db
+    e2e = None
+    if e2e_times:
+        e2e_t = max_over_ranks(pg, statistics.mean(e2e_times))
+        e2e = {"value": round(nrhs * world / e2e_t, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "seconds_per_step": round(e2e_t, 4)}
+
+    # plain FP64 GMG on the same batch
+    plain = None
+    if not a.no_fp64:
+        sp = make_solver(w, G.PREC_FP64, a.tol)
+        ext64 = torch.cuda.ExternalStream(sp.stream)
+        sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext64)
+        _, st64, _ = sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+        e1.record(ext64)
+        e1.synchronize()
+        t64 = max_over_ranks(pg, e0.elapsed_time(e1) / 1e3)
+        ms64, _, by64 = sp.time_smoother(0, reps=2)
+        plain = {"value": round(nrhs * world / t64, 3), "unit": UNIT,
+                 "cycles_mean": float(np.mean([x["cycles"] for x in st64])),
+                 "all_converged": all(x["status"] == "ok" for x in st64),
+                 "smoother_GBps": round(by64 / (ms64 * 1e-3) / 1e9, 1)}
+        sp.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cps = plain["cycles_mean"] if plain else float(np.mean(cycles))
+        nthr = os.cpu_count() or 1
+        v, dt, sample = cpu_sample(w, nthr, cps)
+        cpu = {"value": round(v, 5), "unit": UNIT, "cores": nthr, "kind": "port",
+               "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": round(1e3 * total / a.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 cycles + f64 refinement",
+            "data": "synthetic (seeded log-normal model, no public dataset)",
+            "config": {"workload": f"c3_lognormal_{a.n}^3_25shots_1Hz", "n": a.n,
+                       "rhs_per_step": nrhs, "tol": a.tol, "precision": "mixed",
+                       "smoother": "zebra line relaxation (4 colours), rotating semi-coarsening",
+                       "cycle": "F(1,1)", "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (25 x 128^3 systems, ~12 GB)"},
+            "cycles_mean": float(np.mean(cycles)), "refinements_mean": float(np.mean(refs)),
+            "max_rel_residual": float(max(rels)), "all_converged": ok,
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": round(value / plain["value"], 3) if plain else None,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(sum(launches)), "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def reference_arm(a, rank, world, pg):
+    """The reference's own CPU algorithm (oracle restatement: the reference
+    cannot be built on the GPU machine) on all host threads."""
+    if rank != 0:
+        return
+    from libemmi_mgfd_gb300 import build as B
+    B.build()
+    w = build_workload(a.n)
+    nthr = os.cpu_count() or 1
+    # cycles per solve of this configuration (reference algorithm, 128^3,
+    # to 1e-8): measured by the FP64 GPU run of the same algorithm
+    cps = float(os.environ.get("EMMI_REF_CYCLES", "17"))
+    for _ in range(max(0, a.warmup)):
+        cpu_sample(w, nthr, cps)
+    vals, secs = [], 0.0
+    for _ in range(max(1, a.steps)):
+        v, dt, sample = cpu_sample(w, nthr, cps)
+        vals.append(v)
+        secs += dt
+    value = statistics.mean(vals)
+    line = {
+        "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1e3 * secs / max(1, a.steps), 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded log-normal model, no public dataset)",
+        "config": {"workload": f"c3_lognormal_{a.n}^3_25shots_1Hz", "n": a.n, "tol": a.tol,
+                   "precision": "fp64", "ordering": "lexicographic (the reference's)"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": nthr, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -51,6 +51,9 @@ typedef struct {
                          invmur (emf->sigma11.. after regrid, S/m)          */
   const int *op;    /* [nrhs] operator of each RHS (NULL: rhs i uses op i)  */
   const float *omega; /* [nrhs] angular frequency 2*pi*f (emf->omegas)      */
+  const float *rho_water; /* [nop] smallest model resistivity (emf->rho_water),
+                             used by the Ez receiver conversion; may be NULL
+                             when no extraction is requested                */
 } emmi_problem;
 
 typedef struct {
@@ -100,9 +103,84 @@ double emmi_solver_last_time(const emmi_solver *s);
 long emmi_solver_last_launches(const emmi_solver *s);
 /* Device bytes held by the solver. */
 size_t emmi_solver_device_bytes(const emmi_solver *s);
+/* The CUDA stream (cudaStream_t) every launch of this solver goes to. */
+void *emmi_solver_stream(const emmi_solver *s);
+/* Time `reps` full level-0 line-relaxation sweeps (4 colours, all RHS) along
+ * direction dir with CUDA events on the solver's stream, on the solver's
+ * current fields.  ms: average milliseconds per sweep; launches: kernel
+ * launches per sweep; bytes: algorithmic bytes per sweep,
+ * S*(9c+12)*nrhs with c the complex size (u, f read and u written for three
+ * components, three conductivities per cell). */
+int emmi_solver_time_smoother(emmi_solver *s, int dir, int reps, double *ms,
+                              int *launches, double *bytes);
 void emmi_solver_destroy(emmi_solver *s);
 
 const char *emmi_last_error(void);
+
+/* ---- survey: injection, extraction, gradient (src/inject_extract.c,
+ *      src/build_gradient.c) ------------------------------------------- */
+/* channel codes: 0..2 = Ex,Ey,Ez ; 3..5 = Hx,Hy,Hz */
+typedef struct {
+  int nsrc_ch;        /* source channels (chsrc)                            */
+  const int *src_ch;
+  int nrec_ch;        /* receiver channels (chrec)                          */
+  const int *rec_ch;
+  int nrec;           /* receivers per RHS                                  */
+  const float *src;   /* [nrhs][5]: x, y, z, azimuth (rad), dip (rad)       */
+  const float *rec;   /* [nrhs][nrec][5]                                    */
+} emmi_survey;
+
+/* End-to-end forward modelling of a batch (do_modelling,
+ * src/do_modelling.c:49-67): inject each RHS's source, solve, extract the
+ * receiver data.  Host arrays in and out; dcal: [nrhs][nrec_ch][nrec]
+ * complex float (interleaved).  h2d/d2h (optional) receive the bytes
+ * copied host->device and device->host. */
+int emmi_modelling_batch(emmi_solver *s, const emmi_survey *sv, float *dcal,
+                         emmi_rhs_stats *stats, size_t *h2d, size_t *d2h);
+
+/* Device-resident variants used by the batch path and the drop-in layer.
+ * All pointers are device pointers; fields [nrhs][3*S] complex double. */
+int emmi_inject_sources_dev(emmi_solver *s, const float *src_dev, int nch,
+                            const int *ch, double *b_dev);
+/* adjoint sources from receiver residuals dres_dev [nrhs][nch][nrec]
+ * complex float; m_dev: [nrhs][3*S] complex scratch that receives the
+ * magnetic part M before b += curl M (inject_extract.c:124-314) */
+int emmi_inject_adjoint_dev(emmi_solver *s, const float *rec_dev, int nrec,
+                            int nch, const int *ch, const float *dres_dev,
+                            double *b_dev, double *m_dev);
+/* solve with b already injected into the solver's input buffer (the
+ * buffer emmi_modelling_batch injects into); E stays resident, H is formed
+ * on the device; x_dev/h_dev (optional) receive copies */
+int emmi_solver_solve_resident(emmi_solver *s, double *x_dev, double *h_dev,
+                               emmi_rhs_stats *stats);
+int emmi_extract_receivers_dev(emmi_solver *s, const float *rec_dev, int nrec,
+                               int nch, const int *ch, const double *e_dev,
+                               const double *h_dev, float *dcal_dev);
+
+/* Gradient of the data misfit w.r.t. ln(rho) summed over shots
+ * (build_gradient.c:13-113 and the MPI_Allreduce of fg_fwi.c:265-268, as a
+ * device reduction).  Host arrays: E fields [nshot][nfreq][nz][ny][nx]
+ * complex float for the forward (Ef*) and adjoint (Ea*) solves; rho11,
+ * rho33 [nz][ny][nx]; bathy [ny][nx]; src [nshot][3]; rec [nshot][nrec][3];
+ * idxpar [npar] (1 = rho11/22, 2 = rho33); grad, phess out [npar][nz][ny][nx]
+ * (phess when preco == 1, may be NULL otherwise). */
+int emmi_build_gradient(int nx, int ny, int nz, const float o[3],
+                        const float d[3], int nshot, int nfreq, int npar,
+                        const int *idxpar, int preco, const float *E1f,
+                        const float *E2f, const float *E3f, const float *E1a,
+                        const float *E2a, const float *E3a, const float *rho11,
+                        const float *rho33, const float *bathy, const float *src,
+                        float dsmute, int nrec, const float *rec, float drmute,
+                        float *grad, float *phess);
+
+/* Interpolation of E (from x) or H (from h) to the input model's cell
+ * centres (extract_electric_field / extract_magnetic_field,
+ * inject_extract.c:477-785) for one RHS; host arrays, out [3][nz][ny][nx]
+ * complex float.  rho33 is needed for E (the Ez conversion). */
+int emmi_extract_volume(emmi_solver *s, int rhs, int which /*0=E 1=H*/,
+                        int nx, int ny, int nz, const float o[3],
+                        const float d[3], const float *rho33, const double *field,
+                        float *out);
 
 /* ---- single-operator entry points for parity checks ------------------ */
 /* Each works on one level described by node coordinates (double, n+1 per

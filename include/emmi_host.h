@@ -1,0 +1,69 @@
+/* emmi_host.h -- host front end (C) that prepares the hot path's inputs.
+ *
+ * Restates, in float arithmetic identical to the reference, the regridding
+ * stage that runs before the multigrid solve: padding of the input model,
+ * the source-centred power-law stretched mesh and volume-averaging
+ * homogenization (src/regrid_init_free.c:37-232, src/create_nugrid.c:13-36,
+ * src/homogenization.c:15-111).  All functions are pure: caller-owned
+ * arrays in, caller-owned arrays out.
+ */
+#ifndef EMMI_HOST_H
+#define EMMI_HOST_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EH_OK 0
+#define EH_EINVAL -1
+#define EH_ESEARCH -2 /* the reference's source-depth search would read past
+                         the padded z axis (src/regrid_init_free.c:194 sizes
+                         it by nx); the reference's result is undefined there */
+
+typedef struct {
+  int nx, ny, nz;           /* input model cells                         */
+  float dx, dy, dz;
+  float ox, oy, oz;
+  const float *rho11, *rho22, *rho33; /* [nz][ny][nx] resistivity        */
+  int nb;                   /* padding cells per side (default 10)        */
+  float lextend;            /* padding extent (default 5e4 m)             */
+  float rho_air;            /* default 1e8                                */
+  float d1min, d2min, d3min;/* smallest stretched cells (100, 100, 20)    */
+  int n1, n2, n3;           /* multigrid mesh cells                       */
+} eh_model;
+
+typedef struct {
+  /* node, staggered and spacing arrays, n+1 floats each (emf->x1 ...) */
+  float *x1, *x2, *x3, *x1s, *x2s, *x3s, *d1, *d2, *d3, *d1s, *d2s, *d3s;
+  /* homogenized conductivities and inverse permeability, n3*n2*n1 floats */
+  float *sigma11, *sigma22, *sigma33, *invmur;
+} eh_grid;
+
+/* create_nugrid.c:13-36: x[0..n] of a geometric progression with first cell
+ * dx spanning len; returns the ratio (1 for a uniform grid) */
+float eh_create_nugrid(int n, float len, float dx, float *x);
+
+/* find_index.c:9-30 */
+int eh_find_index(int n, const float *x, float val);
+
+/* regrid_init_free.c:21-34 */
+void eh_stagger(int n, const float *x, float *xs, float *d, float *ds);
+
+/* homogenization.c:15-111: volume averages of in[nz][ny][nx] (on the node
+ * axes xx,yy,zz) over the cells of x1,x2,x3 into out[n3][n2][n1] */
+int eh_homogenize(const float *in, float *out, int nx, int ny, int nz,
+                  const float *xx, const float *yy, const float *zz, int n1,
+                  int n2, int n3, const float *x1, const float *x2,
+                  const float *x3);
+
+/* regrid_init (regrid_init_free.c:37-232) for a source at (sx,sy,sz);
+ * out arrays preallocated by the caller. */
+int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *out);
+
+/* emf_init_free.c:114-128: the smallest resistivity of the three cubes */
+float eh_rho_water(const eh_model *m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

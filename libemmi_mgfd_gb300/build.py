@@ -61,7 +61,9 @@ def build(force: bool = False, verbose: bool = False) -> None:
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+            # the survey kernels reproduce the reference's rounding: no FMA
+            extra = ["-fmad=false"] if src == "emmi_survey.cu" else []
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:

@@ -1,0 +1,246 @@
+/* Host front end of the GB300 hot path: regridding and homogenization.
+ *
+ * Float-for-float restatement of the reference's regrid stage so the mesh
+ * and conductivities fed to the solver are the reference's bit for bit
+ * (checked against tests/golden by tests/test_host_frontend.py):
+ *   create_nugrid   src/create_nugrid.c:13-36
+ *   find_index      src/find_index.c:9-30
+ *   staggering      src/regrid_init_free.c:21-34
+ *   homogenization  src/homogenization.c:15-111
+ *   regrid          src/regrid_init_free.c:37-232
+ */
+#include "emmi_host.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+float eh_create_nugrid(int n, float len, float dx, float *x) {
+  if (n * dx >= len) {
+    for (int i = 0; i <= n; i++) x[i] = i * dx;
+    return 1;
+  }
+  /* ratio q with dx (q^n - 1)/(q - 1) = len by fixed-point iteration in
+   * float, each step evaluated in double (create_nugrid.c:24-33) */
+  float q = 1.1f, qq;
+  const float eps = 1e-15f;
+  for (int it = 0; it < 100000; it++) {
+    qq = pow(len * (q - 1.) / dx + 1., 1. / n);
+    if (fabs(qq - q) < eps) break;
+    q = qq;
+  }
+  x[0] = 0;
+  for (int i = 1; i <= n; i++) x[i] = (pow(q, i) - 1.) * dx / (q - 1.);
+  return q;
+}
+
+int eh_find_index(int n, const float *x, float val) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) / 2;
+    if (x[mid] <= val) lo = mid;
+    if (x[mid] > val) hi = mid;
+    if (lo == hi || lo == hi - 1) break;
+  }
+  return lo;
+}
+
+/* the same search with a bound on the readable length of x; returns -1 if
+ * a probe would fall outside x[0..len-1] */
+static int find_index_checked(int n, const float *x, int len, float val) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) / 2;
+    if (mid >= len) return -1;
+    if (x[mid] <= val) lo = mid;
+    if (x[mid] > val) hi = mid;
+    if (lo == hi || lo == hi - 1) break;
+  }
+  return lo;
+}
+
+void eh_stagger(int n, const float *x, float *xs, float *d, float *ds) {
+  for (int i = 0; i < n; i++) {
+    ds[i] = x[i + 1] - x[i];
+    xs[i] = 0.5 * (x[i] + x[i + 1]);
+  }
+  xs[n] = x[n] + 0.5 * ds[n - 1];
+  ds[n] = xs[n] - x[n];
+  for (int i = 1; i <= n; i++) d[i] = xs[i] - xs[i - 1];
+  d[0] = xs[0] - x[0];
+}
+
+/* one 1D conservative average along an axis: source cells [src[k],src[k+1])
+ * (ns cells) onto target cells [dst[j],dst[j+1]) (nd cells).  `in` and
+ * `out` are read/written with strides. */
+static void average_axis(const float *in, long in_stride, int ns, const float *src, float *out,
+                         long out_stride, int nd, const float *dst) {
+  int i = 0;
+  for (int j = 0; j < nd; j++) {
+    const float a = dst[j], b = dst[j + 1];
+    float s = 0.0;
+    while (i < ns && src[i + 1] <= a) i++;
+    for (int k = i; k < ns && src[k] < b; k++) {
+      const float left = (src[k] > a) ? src[k] : a;
+      const float right = (src[k + 1] < b) ? src[k + 1] : b;
+      const float overlap = right - left;
+      if (overlap > 0.0) s += in[k * in_stride] * overlap;
+    }
+    out[j * out_stride] = s / (b - a);
+  }
+}
+
+int eh_homogenize(const float *in, float *out, int nx, int ny, int nz, const float *xx,
+                  const float *yy, const float *zz, int n1, int n2, int n3, const float *x1,
+                  const float *x2, const float *x3) {
+  float *t1 = malloc((size_t)n1 * ny * nz * sizeof(float));
+  float *t2 = malloc((size_t)n1 * n2 * nz * sizeof(float));
+  if (!t1 || !t2) {
+    free(t1);
+    free(t2);
+    return EH_EINVAL;
+  }
+  /* x, then y, then z: homogenization.c:24-48, 51-76, 79-103 */
+  for (int iz = 0; iz < nz; iz++)
+    for (int iy = 0; iy < ny; iy++)
+      average_axis(in + (size_t)nx * (iy + (size_t)ny * iz), 1, nx, xx,
+                   t1 + (size_t)n1 * (iy + (size_t)ny * iz), 1, n1, x1);
+  for (int iz = 0; iz < nz; iz++)
+    for (int ix = 0; ix < n1; ix++)
+      average_axis(t1 + ix + (size_t)n1 * ny * iz, n1, ny, yy, t2 + ix + (size_t)n1 * n2 * iz, n1,
+                   n2, x2);
+  for (int iy = 0; iy < n2; iy++)
+    for (int ix = 0; ix < n1; ix++)
+      average_axis(t2 + ix + (size_t)n1 * iy, (long)n1 * n2, nz, zz, out + ix + (size_t)n1 * iy,
+                   (long)n1 * n2, n3, x3);
+  free(t1);
+  free(t2);
+  return EH_OK;
+}
+
+float eh_rho_water(const eh_model *m) {
+  const long n = (long)m->nx * m->ny * m->nz;
+  float vmin = m->rho11[0];
+  for (long i = 0; i < n; i++) {
+    if (m->rho11[i] < vmin) vmin = m->rho11[i];
+    if (m->rho22[i] < vmin) vmin = m->rho22[i];
+    if (m->rho33[i] < vmin) vmin = m->rho33[i];
+  }
+  return vmin;
+}
+
+/* padded axis: nb geometric cells on each side of n uniform cells
+ * (regrid_init_free.c:47-70) */
+static void padded_axis(int n, float d, float o, int nb, float lextend, float *ax) {
+  float *x = malloc((nb + 1) * sizeof(float));
+  for (int i = 0; i <= n; i++) ax[i + nb] = o + i * d;
+  eh_create_nugrid(nb, lextend, d, x);
+  for (int i = 0; i <= nb; i++) {
+    ax[i] = o - x[nb - i];
+    ax[i + n + nb] = o + n * d + x[i];
+  }
+  free(x);
+}
+
+/* stretched mesh axis centred on the source: n/2 cells to the low side and
+ * the rest to the high side (regrid_init_free.c:156-187) */
+static void centred_axis(int n, float src, float lo, float hi, float dmin, float *out) {
+  const int np1 = n / 2, np2 = n - np1;
+  float *x = malloc((n + 1) * sizeof(float));
+  eh_create_nugrid(np1, src - lo, dmin, x);
+  for (int i = 0; i <= np1; i++) out[np1 - i] = src - x[i];
+  eh_create_nugrid(np2, hi - src, dmin, x);
+  for (int i = 0; i <= np2; i++) out[np1 + i] = src + x[i];
+  free(x);
+}
+
+int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *g) {
+  if (!m || !g || m->nx < 1 || m->ny < 1 || m->nz < 1 || m->nb < 0 || m->n1 < 2 || m->n2 < 2 ||
+      m->n3 < 2)
+    return EH_EINVAL;
+  const int nb = m->nb;
+  const int nxp = m->nx + 2 * nb, nyp = m->ny + 2 * nb, nzp = m->nz + 2 * nb;
+  float *xx = malloc((nxp + 1) * sizeof(float));
+  float *yy = malloc((nyp + 1) * sizeof(float));
+  float *zz = malloc((nzp + 1) * sizeof(float));
+  padded_axis(m->nx, m->dx, m->ox, nb, m->lextend, xx);
+  padded_axis(m->ny, m->dy, m->oy, nb, m->lextend, yy);
+  padded_axis(m->nz, m->dz, m->oz, nb, m->lextend, zz);
+
+  /* padded model: interior copied (sigma = 1/rho for 11/22, rho for 33),
+   * edges replicated, nb air cells on top (regrid_init_free.c:82-141) */
+  const size_t np = (size_t)nxp * nyp * nzp;
+  float *pad[3];
+  for (int a = 0; a < 3; a++) pad[a] = malloc(np * sizeof(float));
+#define PAD(a, i, j, k) pad[a][(i) + (size_t)nxp * ((j) + (size_t)nyp * (k))]
+  for (int k = 0; k < m->nz; k++)
+    for (int j = 0; j < m->ny; j++)
+      for (int i = 0; i < m->nx; i++) {
+        const size_t c = i + (size_t)m->nx * (j + (size_t)m->ny * k);
+        PAD(0, i + nb, j + nb, k + nb) = 1. / m->rho11[c];
+        PAD(1, i + nb, j + nb, k + nb) = 1. / m->rho22[c];
+        PAD(2, i + nb, j + nb, k + nb) = m->rho33[c];
+      }
+  for (int a = 0; a < 3; a++) {
+    for (int k = 0; k < nzp; k++)
+      for (int j = 0; j < nyp; j++)
+        for (int i = 0; i < nb; i++) {
+          PAD(a, i, j, k) = PAD(a, nb, j, k);
+          PAD(a, nxp - 1 - i, j, k) = PAD(a, nxp - 1 - nb, j, k);
+        }
+    for (int k = 0; k < nzp; k++)
+      for (int j = 0; j < nb; j++)
+        for (int i = 0; i < nxp; i++) {
+          PAD(a, i, j, k) = PAD(a, i, nb, k);
+          PAD(a, i, nyp - 1 - j, k) = PAD(a, i, nyp - 1 - nb, k);
+        }
+    for (int k = 0; k < nb; k++)
+      for (int j = 0; j < nyp; j++)
+        for (int i = 0; i < nxp; i++) {
+          PAD(a, i, j, k) = (a < 2) ? (float)(1. / m->rho_air) : m->rho_air;
+          PAD(a, i, j, nzp - 1 - k) = PAD(a, i, j, nzp - 1 - nb);
+        }
+  }
+#undef PAD
+  int rc = EH_OK;
+  centred_axis(m->n1, sx, xx[0], xx[nxp], m->d1min, g->x1);
+  centred_axis(m->n2, sy, yy[0], yy[nyp], m->d2min, g->x2);
+  /* z: input-model nodes down to 5 cells below the source, then stretched
+   * to the bottom (regrid_init_free.c:190-205).  The reference sizes the
+   * source search by nx (its line 194); it is reproduced, with a check that
+   * the search stays on the padded z axis. */
+  const int k0 = find_index_checked(m->nx + 2 * nb, zz, nzp + 1, sz);
+  if (k0 < 0) {
+    rc = EH_ESEARCH;
+  } else {
+    const int np1 = k0 + 5, np2 = m->n3 - np1;
+    if (np1 > nzp || np2 < 1) {
+      rc = EH_EINVAL;
+    } else {
+      for (int i = 0; i <= np1; i++) g->x3[i] = zz[i];
+      float *x = malloc((np2 + 1) * sizeof(float));
+      eh_create_nugrid(np2, zz[nzp] - g->x3[np1], m->d3min, x);
+      for (int i = 0; i <= np2; i++) g->x3[np1 + i] = g->x3[np1] + x[i];
+      free(x);
+    }
+  }
+  if (rc == EH_OK) {
+    eh_stagger(m->n1, g->x1, g->x1s, g->d1, g->d1s);
+    eh_stagger(m->n2, g->x2, g->x2s, g->d2, g->d2s);
+    eh_stagger(m->n3, g->x3, g->x3s, g->d3, g->d3s);
+    float *outs[3] = {g->sigma11, g->sigma22, g->sigma33};
+    for (int a = 0; a < 3 && rc == EH_OK; a++)
+      rc = eh_homogenize(pad[a], outs[a], nxp, nyp, nzp, xx, yy, zz, m->n1, m->n2, m->n3, g->x1,
+                         g->x2, g->x3);
+    const size_t nc = (size_t)m->n1 * m->n2 * m->n3;
+    for (size_t c = 0; c < nc; c++) {
+      g->sigma33[c] = 1. / g->sigma33[c]; /* rho33 average -> sigma33 */
+      g->invmur[c] = 1.;
+    }
+  }
+  for (int a = 0; a < 3; a++) free(pad[a]);
+  free(xx);
+  free(yy);
+  free(zz);
+  return rc;
+}

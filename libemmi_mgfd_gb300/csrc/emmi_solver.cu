@@ -28,15 +28,13 @@
 #include <vector>
 
 #include "emmi_gpu.h"
-#include "emmi_kernels.cuh"
+#include "emmi_solver_impl.cuh"
 
 using namespace emmi;
 
-namespace {
+static thread_local std::string g_err;
 
-thread_local std::string g_err;
-
-void set_err(const char* fmt, ...) {
+void emmi::set_err(const char* fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -44,6 +42,9 @@ void set_err(const char* fmt, ...) {
   va_end(ap);
   g_err = buf;
 }
+
+namespace {
+
 
 #define CK(x)                                                                     \
   do {                                                                            \
@@ -54,8 +55,6 @@ void set_err(const char* fmt, ...) {
     }                                                                             \
   } while (0)
 
-constexpr double kMu0 = 4. * 3.14159265358979323846264 * 1e-7;  // include/cstd.h:38-40
-constexpr int kMaxLev = 24;
 
 // gmg.c:1688-1699
 int depth_of(int n) {
@@ -80,11 +79,6 @@ void stagger(int n, const double* x, double* xs, double* d, double* ds) {
   d[0] = xs[0] - x[0];
 }
 
-struct HLev {
-  int n[3];
-  int sc[3];
-  long S, ncell;
-};
 
 // ------------------------------------------------------------ setup kernels
 // cells64 = raw * vol, vol = d1s*d2s*d3s (gmg.c:1795-1799); sigmas floored at
@@ -200,53 +194,6 @@ inline unsigned blocks_for(long n, int bs = 256, long cap = 65535) {
 
 }  // namespace
 
-// ============================================================ solver state
-struct emmi_solver {
-  emmi_options opt;
-  int n[3];
-  int nop, nrhs, lmax;
-  int gmax1, gstride;
-  HLev hier[3][kMaxLev];
-  bool has_norm;  // the cycle has a level-0 norm test
-
-  // device memory
-  std::vector<void*> allocs;
-  size_t bytes = 0;
-  int* d_op = nullptr;
-  int* d_active = nullptr;  // cycling RHS
-  int* d_refine = nullptr;  // RHS refining now (MIXED)
-  double* d_wmu64 = nullptr;
-  float* d_wmu32 = nullptr;
-  double* d_norm = nullptr;   // level-0 norm^2 per RHS (cycle)
-  double* d_norm64 = nullptr; // FP64 refinement norm^2 per RHS
-  double* geo64[3][kMaxLev] = {};
-  float* geo32[3][kMaxLev] = {};
-  double* cells64[3][kMaxLev] = {};
-  float* cells32[3][kMaxLev] = {};
-  double2 *u64[kMaxLev] = {}, *f64[kMaxLev] = {}, *r64[kMaxLev] = {};
-  float2 *u32[kMaxLev] = {}, *f32[kMaxLev] = {}, *r32[kMaxLev] = {};
-  void* scratch = nullptr;
-  size_t scratch_bytes = 0;
-  int chunk = 1;  // RHS per line-sweep launch (scratch bound)
-
-  cudaStream_t st = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaGraphExec_t gA[3] = {}, gB[3] = {};
-  long nodesA[3] = {}, nodesB[3] = {};
-  double last_time = 0;
-  long last_launches = 0;
-  long launch_counter = 0;
-
-  // host mirrors
-  std::vector<int> h_active, h_refine;
-
-  template <typename T> LevelView<T> view(int h, int l) const;
-  template <typename T> void emit_smooth(int h, int l, int iter);
-  template <typename T> void emit_cycle(int h, int l, int kind, int want, int& cur);
-  template <typename T> void emit_residual0(int want, int& cur);
-  template <typename T> int build_graphs();
-  int alloc(void** p, size_t b);
-};
 
 int emmi_solver::alloc(void** p, size_t b) {
   if (b == 0) b = 16;
@@ -608,6 +555,42 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     float* raw = nullptr;
     TRY(s->alloc((void**)&raw, (size_t)s->nop * 4 * nc0 * sizeof(float)));
     CKS(cudaMemcpy(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float), cudaMemcpyHostToDevice));
+    s->raw_cells = raw;
+    // survey grids in float as emf_t holds them (regrid_init_free.c:21-34)
+    {
+      std::vector<float> sg((size_t)s->nop * s->gstride, 0.f);
+      for (int o = 0; o < s->nop; o++) {
+        float* G = sg.data() + (size_t)o * s->gstride;
+        for (int e = 0; e < 3; e++) {
+          const int ne = s->n[e];
+          const float* src = e == 0 ? P->x1 : e == 1 ? P->x2 : P->x3;
+          float* x = G + e * s->gmax1;
+          float* xs = G + (3 + e) * s->gmax1;
+          float* d = G + (6 + e) * s->gmax1;
+          std::vector<float> ds(ne + 1);
+          for (int i = 0; i <= ne; i++) x[i] = src[(size_t)o * (ne + 1) + i];
+          for (int i = 0; i < ne; i++) {
+            ds[i] = x[i + 1] - x[i];
+            xs[i] = 0.5 * (x[i] + x[i + 1]);
+          }
+          xs[ne] = x[ne] + 0.5 * ds[ne - 1];
+          for (int i = 1; i <= ne; i++) d[i] = xs[i] - xs[i - 1];
+          d[0] = xs[0] - x[0];
+        }
+      }
+      TRY(s->alloc((void**)&s->sgeo, sg.size() * sizeof(float)));
+      CKS(cudaMemcpy(s->sgeo, sg.data(), sg.size() * sizeof(float), cudaMemcpyHostToDevice));
+      std::vector<float> rw(s->nop, 0.f);
+      if (P->rho_water)
+        for (int o = 0; o < s->nop; o++) rw[o] = P->rho_water[o];
+      TRY(s->alloc((void**)&s->d_rho_water, s->nop * sizeof(float)));
+      CKS(cudaMemcpy(s->d_rho_water, rw.data(), s->nop * sizeof(float), cudaMemcpyHostToDevice));
+      s->h_omega.assign(P->omega, P->omega + s->nrhs);
+      TRY(s->alloc((void**)&s->d_omega, s->nrhs * sizeof(float)));
+      CKS(cudaMemcpy(s->d_omega, P->omega, s->nrhs * sizeof(float), cudaMemcpyHostToDevice));
+      s->h_op.resize(s->nrhs);
+      for (int r = 0; r < s->nrhs; r++) s->h_op[r] = P->op ? P->op[r] : r;
+    }
     // true operator in FP64 at level 0 (both modes)
     TRY(s->alloc((void**)&s->cells64[0][0], (size_t)s->nop * 4 * nc0 * sizeof(double)));
     dim3 g0(blocks_for(nc0), s->nop);
@@ -733,9 +716,11 @@ static int read_norms(emmi_solver* s, const double* dev, std::vector<double>& ho
   return EMMI_OK;
 }
 
-int emmi_solver_solve(emmi_solver* s, const double* b, double* x, double* h, int device,
-                      emmi_rhs_stats* stats) {
-  if (!s || !b || !x) {
+// resident: b is already in u64[0]; x/h may be null (E stays in u64[0],
+// H is always formed in f64[0] for the extraction that follows)
+static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int device,
+                      emmi_rhs_stats* stats, bool resident) {
+  if (!s || (!resident && (!b || !x))) {
     set_err("emmi_solver_solve: null argument");
     return EMMI_EINVAL;
   }
@@ -749,10 +734,12 @@ int emmi_solver_solve(emmi_solver* s, const double* b, double* x, double* h, int
   CK(cudaEventRecord(s->ev0, s->st));
   // b -> device (into u64[0] temporarily), then f64[0] = b * dual volume
   double2* bdev = s->u64[0];
-  if (device)
-    CK(cudaMemcpyAsync(bdev, b, fbytes, cudaMemcpyDeviceToDevice, s->st));
-  else
-    CK(cudaMemcpyAsync(bdev, b, fbytes, cudaMemcpyHostToDevice, s->st));
+  if (!resident) {
+    if (device)
+      CK(cudaMemcpyAsync(bdev, b, fbytes, cudaMemcpyDeviceToDevice, s->st));
+    else
+      CK(cudaMemcpyAsync(bdev, b, fbytes, cudaMemcpyHostToDevice, s->st));
+  }
   {
     dim3 g(blocks_for(S), nrhs);
     k_scale_dual<<<g, 256, 0, s->st>>>(bdev, s->f64[0], s->geo64[0][0], s->d_op, s->gstride,
@@ -947,19 +934,21 @@ int emmi_solver_solve(emmi_solver* s, const double* b, double* x, double* h, int
     }
   }
   // outputs: x = E, h = curl E / (i w mu0) (gmg.c:1927-1929)
-  if (device)
-    CK(cudaMemcpyAsync(x, s->u64[0], fbytes, cudaMemcpyDeviceToDevice, s->st));
-  else
-    CK(cudaMemcpyAsync(x, s->u64[0], fbytes, cudaMemcpyDeviceToHost, s->st));
-  if (h) {
+  if (x) {
+    if (device)
+      CK(cudaMemcpyAsync(x, s->u64[0], fbytes, cudaMemcpyDeviceToDevice, s->st));
+    else
+      CK(cudaMemcpyAsync(x, s->u64[0], fbytes, cudaMemcpyDeviceToHost, s->st));
+  }
+  if (h || resident) {
     // H goes to f64[0] (b*vol is no longer needed) then out
     dim3 g(blocks_for(S), nrhs);
     k_curl_h<<<g, 256, 0, s->st>>>(s->u64[0], s->f64[0], s->geo64[0][0], s->d_op, s->d_wmu64,
                                    s->gstride, s->gmax1, s->n[0], s->n[1], s->n[2]);
     s->last_launches++;
-    if (device)
+    if (h && device)
       CK(cudaMemcpyAsync(h, s->f64[0], fbytes, cudaMemcpyDeviceToDevice, s->st));
-    else
+    else if (h)
       CK(cudaMemcpyAsync(h, s->f64[0], fbytes, cudaMemcpyDeviceToHost, s->st));
   }
   CK(cudaEventRecord(s->ev1, s->st));
@@ -976,6 +965,78 @@ int emmi_solver_solve(emmi_solver* s, const double* b, double* x, double* h, int
       stats[r].rnorm = rn[r];
       stats[r].refinements = nref[r];
     }
+  return EMMI_OK;
+}
+
+int emmi_solver_solve(emmi_solver* s, const double* b, double* x, double* h, int device,
+                      emmi_rhs_stats* stats) {
+  return solve_impl(s, b, x, h, device, stats, false);
+}
+
+int emmi_solver_solve_resident(emmi_solver* s, double* x_dev, double* h_dev,
+                               emmi_rhs_stats* stats) {
+  return solve_impl(s, nullptr, x_dev, h_dev, 1, stats, true);
+}
+
+void* emmi_solver_stream(const emmi_solver* s) { return s ? (void*)s->st : nullptr; }
+
+int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int* launches,
+                              double* bytes) {
+  if (!s || dir < 0 || dir > 2 || reps < 1 || s->lmax < 2) {
+    set_err("emmi_solver_time_smoother: bad argument");
+    return EMMI_EINVAL;
+  }
+  // the hierarchy whose level 1 coarsens `dir` (its uncoarsened direction
+  // is another one), so level 0 relaxes lines along dir
+  int h = -1;
+  for (int c = 0; c < 3 && h < 0; c++)
+    if (s->hier[c][1].sc[dir] == 2) h = c;
+  if (h < 0) {
+    set_err("emmi_solver_time_smoother: direction %d is never coarsened", dir);
+    return EMMI_EINVAL;
+  }
+  const bool mixed = s->opt.precision == EMMI_PREC_MIXED;
+  std::vector<int> all(s->nrhs, 1);
+  CK(cudaMemcpyAsync(s->d_active, all.data(), s->nrhs * sizeof(int), cudaMemcpyHostToDevice, s->st));
+  auto sweep = [&]() {
+    for (int cc = 0; cc < 4; cc++)
+      for (int r0 = 0; r0 < s->nrhs; r0 += s->chunk) {
+        const int nr = std::min(s->chunk, s->nrhs - r0);
+        if (mixed) {
+          LevelView<float> W = s->view<float>(h, 0);
+          W.nrhs = nr;
+          W.u += (long)r0 * 3 * W.S;
+          W.f += (long)r0 * 3 * W.S;
+          W.r += (long)r0 * 3 * W.S;
+          W.wmu += r0;
+          W.active += r0;
+          W.op += r0;
+          launch_line_sweep<float>(W, dir, cc, (C_t<float>*)s->scratch, s->st);
+        } else {
+          LevelView<double> W = s->view<double>(h, 0);
+          W.nrhs = nr;
+          W.u += (long)r0 * 3 * W.S;
+          W.f += (long)r0 * 3 * W.S;
+          W.r += (long)r0 * 3 * W.S;
+          W.wmu += r0;
+          W.active += r0;
+          W.op += r0;
+          launch_line_sweep<double>(W, dir, cc, (C_t<double>*)s->scratch, s->st);
+        }
+      }
+  };
+  sweep();  // warm
+  CK(cudaEventRecord(s->ev0, s->st));
+  for (int i = 0; i < reps; i++) sweep();
+  CK(cudaEventRecord(s->ev1, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaGetLastError());
+  float t = 0;
+  cudaEventElapsedTime(&t, s->ev0, s->ev1);
+  const double c = mixed ? 8.0 : 16.0;
+  if (ms) *ms = t / reps;
+  if (launches) *launches = 4 * ((s->nrhs + s->chunk - 1) / s->chunk);
+  if (bytes) *bytes = (double)s->hier[0][0].S * (9 * c + 12) * s->nrhs;
   return EMMI_OK;
 }
 

@@ -33,7 +33,17 @@ class EmmiError(RuntimeError):
 class _Problem(C.Structure):
     _fields_ = [("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int), ("nop", C.c_int),
                 ("nrhs", C.c_int), ("x1", C.c_void_p), ("x2", C.c_void_p), ("x3", C.c_void_p),
-                ("cells", C.c_void_p), ("op", C.c_void_p), ("omega", C.c_void_p)]
+                ("cells", C.c_void_p), ("op", C.c_void_p), ("omega", C.c_void_p),
+                ("rho_water", C.c_void_p)]
+
+
+class _Survey(C.Structure):
+    _fields_ = [("nsrc_ch", C.c_int), ("src_ch", C.c_void_p), ("nrec_ch", C.c_int),
+                ("rec_ch", C.c_void_p), ("nrec", C.c_int), ("src", C.c_void_p),
+                ("rec", C.c_void_p)]
+
+
+CHANNELS = {"Ex": 0, "Ey": 1, "Ez": 2, "Hx": 3, "Hy": 4, "Hz": 5}
 
 
 class _Options(C.Structure):
@@ -107,7 +117,7 @@ class Solver:
     [nop, 4, n3, n2, n1]; omega: float32 [nrhs]; op: int [nrhs] or None."""
 
     def __init__(self, n: Sequence[int], x1, x2, x3, cells, omega, op=None,
-                 options: Optional[Options] = None):
+                 options: Optional[Options] = None, rho_water=None):
         self.n = tuple(int(v) for v in n)
         self.x1 = np.ascontiguousarray(np.atleast_2d(x1), np.float32)
         self.x2 = np.ascontiguousarray(np.atleast_2d(x2), np.float32)
@@ -120,9 +130,12 @@ class Solver:
         self.options = options or Options()
         n1, n2, n3 = self.n
         self.nslots = (n1 + 1) * (n2 + 1) * (n3 + 1)
+        self.rho_water = (np.zeros(self.nop, np.float32) if rho_water is None else
+                          np.ascontiguousarray(np.broadcast_to(rho_water, (self.nop,)), np.float32))
         prob = _Problem(n1, n2, n3, self.nop, self.nrhs, _p(self.x1).value, _p(self.x2).value,
                         _p(self.x3).value, _p(self.cells).value,
-                        None if self.op is None else _p(self.op).value, _p(self.omega).value)
+                        None if self.op is None else _p(self.op).value, _p(self.omega).value,
+                        _p(self.rho_water).value)
         h = C.c_void_p()
         _check(lib().emmi_solver_create(C.byref(h), C.byref(prob), C.byref(self.options._c())),
                "emmi_solver_create")
@@ -145,11 +158,61 @@ class Solver:
                "emmi_solver_solve")
         return x, h, self._stats(st)
 
+    def modelling(self, src, rec, chsrc=("Ex",), chrec=("Ex", "Ey", "Hx", "Hy")):
+        """Inject, solve and extract for every RHS (do_modelling as one batch).
+        src: [nrhs, 5] x,y,z,azimuth(rad),dip(rad); rec: [nrhs, nrec, 5] or
+        [nrec, 5] shared.  Returns (dcal [nrhs, nch, nrec] complex64, stats,
+        (h2d_bytes, d2h_bytes))."""
+        src = np.ascontiguousarray(np.broadcast_to(src, (self.nrhs, 5)), np.float32)
+        rec = np.asarray(rec, np.float32)
+        if rec.ndim == 2:
+            rec = np.broadcast_to(rec, (self.nrhs,) + rec.shape)
+        rec = np.ascontiguousarray(rec, np.float32)
+        nrec = rec.shape[1]
+        cs = np.array([CHANNELS[c] for c in chsrc], np.int32)
+        cr = np.array([CHANNELS[c] for c in chrec], np.int32)
+        sv = _Survey(len(cs), _p(cs).value, len(cr), _p(cr).value, nrec, _p(src).value,
+                     _p(rec).value)
+        out = np.zeros((self.nrhs, len(cr), nrec), np.complex64)
+        st = (_Stats * self.nrhs)()
+        h2d, d2h = C.c_size_t(), C.c_size_t()
+        _check(lib().emmi_modelling_batch(self._h, C.byref(sv), _p(out), st, C.byref(h2d),
+                                          C.byref(d2h)), "emmi_modelling_batch")
+        return out, self._stats(st), (h2d.value, d2h.value)
+
+    def extract_volume(self, rhs, which, nxyz, o, d, field, rho33=None):
+        """E (which=0, from x) or H (which=1, from h) at the input cell centres:
+        three complex64 arrays [nz, ny, nx]."""
+        nx, ny, nz = (int(v) for v in nxyz)
+        out = np.zeros((3, nz, ny, nx), np.complex64)
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        f = np.ascontiguousarray(field, np.complex128)
+        r33 = None if rho33 is None else np.ascontiguousarray(rho33, np.float32)
+        _check(lib().emmi_extract_volume(self._h, int(rhs), int(which), nx, ny, nz, _p(o), _p(d),
+                                         None if r33 is None else _p(r33), _p(f), _p(out)),
+               "emmi_extract_volume")
+        return list(out)
+
     @staticmethod
     def _stats(st):
         return [dict(cycles=s.cycles, status=STATUS.get(s.status, s.status), rnorm0=s.rnorm0,
                      rnorm=s.rnorm, rel=(s.rnorm / s.rnorm0 if s.rnorm0 > 0 else 0.0),
                      refinements=s.refinements) for s in st]
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of the solver (for torch.cuda.ExternalStream)."""
+        lib().emmi_solver_stream.restype = C.c_void_p
+        return int(lib().emmi_solver_stream(self._h) or 0)
+
+    def time_smoother(self, direction: int, reps: int = 5):
+        """(ms per level-0 line sweep, launches per sweep, algorithmic bytes)."""
+        ms, nl, by = C.c_double(), C.c_int(), C.c_double()
+        _check(lib().emmi_solver_time_smoother(self._h, int(direction), int(reps), C.byref(ms),
+                                               C.byref(nl), C.byref(by)),
+               "emmi_solver_time_smoother")
+        return ms.value, nl.value, by.value
 
     @property
     def last_time(self) -> float:
@@ -203,3 +266,32 @@ def level_smooth(n, x, cells, omega, u, f, direction, prec=PREC_FP64, iter=0):
                                    prec, int(direction), int(iter), _p(u), _p(f)),
            "emmi_level_smooth")
     return u
+
+
+def build_gradient(nxyz, o, d, idxpar, preco, Ef, Ea, rho11, rho33, bathy, src, rec,
+                   dsmute=800.0, drmute=200.0):
+    """Gradient w.r.t. ln(rho) summed over shots on the device.
+    Ef/Ea: three arrays [nshot, nfreq, nz, ny, nx] complex64 each;
+    src [nshot, 3]; rec [nshot, nrec, 3].  Returns (grad, phess)."""
+    nx, ny, nz = (int(v) for v in nxyz)
+    Ef = [np.ascontiguousarray(a, np.complex64) for a in Ef]
+    Ea = [np.ascontiguousarray(a, np.complex64) for a in Ea]
+    nshot = Ef[0].shape[0]
+    nfreq = Ef[0].size // (nshot * nx * ny * nz)
+    idx = np.ascontiguousarray(idxpar, np.int32)
+    npar = len(idx)
+    grad = np.zeros((npar, nz, ny, nx), np.float32)
+    phess = np.zeros((npar, nz, ny, nx), np.float32)
+    src = np.ascontiguousarray(np.asarray(src, np.float32)[..., :3].reshape(nshot, 3))
+    rec = np.asarray(rec, np.float32)[..., :3]
+    nrec = rec.shape[-2] if rec.size else 0
+    rec = np.ascontiguousarray(np.broadcast_to(rec, (nshot, nrec, 3)), np.float32)
+    o = np.ascontiguousarray(o, np.float32)
+    d = np.ascontiguousarray(d, np.float32)
+    keep = [np.ascontiguousarray(a, np.float32) for a in (rho11, rho33, bathy)]
+    _check(lib().emmi_build_gradient(nx, ny, nz, _p(o), _p(d), nshot, nfreq, npar, _p(idx),
+                                     int(preco), *[_p(a) for a in Ef], *[_p(a) for a in Ea],
+                                     *[_p(a) for a in keep], _p(src), C.c_float(dsmute), nrec,
+                                     _p(rec), C.c_float(drmute), _p(grad), _p(phess)),
+           "emmi_build_gradient")
+    return grad, phess
