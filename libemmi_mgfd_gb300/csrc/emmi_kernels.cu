@@ -191,16 +191,62 @@ void launch_norm(const C_t<T>* v, long n3s, int nrhs, const int* active, double*
 }
 
 // ------------------------------------------------------------ line sweep
+// One colour of line relaxation along D is three launches:
+//   assemble  thread per (line, node): for the rows of the node, the lower
+//             band entries (offsets -5..-1, real), the complex diagonal and
+//             the current residual, into a record buffer [row][line][12];
+//             threads run along the contiguous memory direction so every
+//             stencil load is coalesced
+//   solve     thread per line: streaming complex-symmetric LDL^T over its
+//             records (factors written in place), then back substitution;
+//             records of one row are contiguous across lines (coalesced)
+//   apply     thread per (line, node): u += correction, coalesced like
+//             assemble
+// Record of one row, T-typed: [0..4] band, [5,6] diagonal, [7,8] residual;
+// after the forward pass [0..9] = l_1..l_5 (complex), [10,11] = z; after the
+// backward pass [10,11] = the correction x.
 #define WI(i, j) ((i) * ((i) + 1) / 2 + (j))
+constexpr int kRec = 12;
 
-// assemble the row (type TT, component C) at node s of line (ta,tb) into
-// window slot 5: lower band entries (offsets -5..-1), complex diagonal and the
-// current residual of the row.
+struct LineGeom {
+  int la, lb, fa, fb;  // lines per transverse direction and first index
+  long nl;             // lines of the colour
+  int nd, m;           // nodes along the line, rows
+};
+
+template <int D>
+__device__ __forceinline__ LineGeom line_geom(const int n[3], int pa, int pb) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  LineGeom g;
+  g.fa = pa ? 1 : 2;
+  g.fb = pb ? 1 : 2;
+  g.la = (n[A] - 1 >= g.fa) ? (n[A] - 1 - g.fa) / 2 + 1 : 0;
+  g.lb = (n[B] - 1 >= g.fb) ? (n[B] - 1 - g.fb) / 2 + 1 : 0;
+  g.nl = (long)g.la * g.lb;
+  g.nd = n[D];
+  g.m = 5 * n[D] - 4;
+  return g;
+}
+
+// work item -> (line, node s); threads along memory-contiguous direction
+template <int D>
+__device__ __forceinline__ bool line_item(const LineGeom& g, long id, long& l, int& s) {
+  if (id >= g.nl * g.nd) return false;
+  if (D == 0) {  // rows of an x-line are contiguous in memory
+    l = id / g.nd;
+    s = 1 + (int)(id % g.nd);
+  } else {  // neighbouring lines (consecutive i) are contiguous
+    l = id % g.nl;
+    s = 1 + (int)(id / g.nl);
+  }
+  return true;
+}
+
 template <typename T, int D, int TT, int C>
-__device__ __forceinline__ void line_row(const LevelView<T>& L, const C_t<T>* u, const C_t<T>* f,
-                                         const T* cells, const Geo<T>& G, T wmu, int ta, int tb,
-                                         int s, int row, const long ss[3], C_t<T> (&W)[21],
-                                         C_t<T> (&y)[6]) {
+__device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>* u,
+                                             const C_t<T>* f, const T* cells, const Geo<T>& G,
+                                             T wmu, int ta, int tb, int s, int row,
+                                             const long ss[3], T* __restrict__ rec) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   int P[3];
   P[D] = (TT == 0) ? s - 1 : s;
@@ -209,20 +255,24 @@ __device__ __forceinline__ void line_row(const LevelView<T>& L, const C_t<T>* u,
   const long sl = slot_id(L.n, P[0], P[1], P[2]);
   EdgeCoef<T> e;
   const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
-  y[5] = csub<T>(f[(long)C * L.S + sl], au);
-#pragma unroll
-  for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
-  W[WI(5, 5)] = mk<T>(e.dre, e.dim);
+  const C_t<T> r = csub<T>(f[(long)C * L.S + sl], au);
+  T band[5] = {0, 0, 0, 0, 0};
 #define LINE_ENTRY(K)                                                         \
   {                                                                           \
     constexpr int off = line_off(D, TT, K);                                   \
     if constexpr (off < 0) {                                                  \
-      if (row + off >= 0) W[WI(5, 5 + off)] = mk<T>(e.c[K], 0);               \
+      if (row + off >= 0) band[5 + off] = e.c[K];                             \
     }                                                                         \
   }
   LINE_ENTRY(0) LINE_ENTRY(1) LINE_ENTRY(2) LINE_ENTRY(3) LINE_ENTRY(4) LINE_ENTRY(5)
   LINE_ENTRY(6) LINE_ENTRY(7) LINE_ENTRY(8) LINE_ENTRY(9) LINE_ENTRY(10) LINE_ENTRY(11)
 #undef LINE_ENTRY
+#pragma unroll
+  for (int i = 0; i < 5; i++) rec[i] = band[i];
+  rec[5] = e.dre;
+  rec[6] = e.dim;
+  rec[7] = r.x;
+  rec[8] = r.y;
 }
 
 template <int D, int TT>
@@ -237,30 +287,50 @@ __device__ __forceinline__ long line_slot(const int n[3], long S, int ta, int tb
 }
 
 template <typename T, int D>
-__global__ void __launch_bounds__(128) k_line_sweep(LevelView<T> L, int pa, int pb,
-                                                    C_t<T>* __restrict__ scr) {
+__global__ void __launch_bounds__(256) k_line_assemble(LevelView<T> L, int pa, int pb,
+                                                       T* __restrict__ buf) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   const int rhs = blockIdx.y;
   if (L.active && !L.active[rhs]) return;
-  const int fa = pa ? 1 : 2, fb = pb ? 1 : 2;
-  const int la = (L.n[A] - 1 >= fa) ? (L.n[A] - 1 - fa) / 2 + 1 : 0;
-  const int lb = (L.n[B] - 1 >= fb) ? (L.n[B] - 1 - fb) / 2 + 1 : 0;
-  const long nl = (long)la * lb;
-  const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (l >= nl) return;
-  const int ta = fa + 2 * (int)(l % la), tb = fb + 2 * (int)(l / la);
-  const long stride = nl * gridDim.y;
-  const long gid = (long)rhs * nl + l;
-  const int nd = L.n[D];
-  const int m = 5 * nd - 4;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  long l;
+  int s;
+  if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
+  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
-  C_t<T>* u = L.u + (long)rhs * 3 * L.S;
+  const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
   const C_t<T>* f = L.f + (long)rhs * 3 * L.S;
   const T* cells = L.cells + (long)op_of(L, rhs) * 4 * L.ncell;
   const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
   const T wmu = L.wmu[rhs];
+  T* base = buf + (long)rhs * g.m * g.nl * kRec;
+  const int r0 = 5 * (s - 1);
+  auto rec = [&](int row) { return base + ((long)row * g.nl + l) * kRec; };
+  assemble_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0));
+  if (s < g.nd) {
+    assemble_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1));
+    assemble_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2));
+    assemble_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3));
+    assemble_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4));
+  }
+}
 
+template <typename T>
+__device__ __forceinline__ void load_rec9(const T* p, T (&v)[9]) {
+#pragma unroll
+  for (int i = 0; i < 9; i++) v[i] = p[i];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ active, long nl, int m,
+                                                    T* __restrict__ buf) {
+  const int rhs = blockIdx.y;
+  if (active && !active[rhs]) return;
+  const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (l >= nl) return;
+  T* base = buf + (long)rhs * m * nl * kRec + l * kRec;
+  const long rs = nl * kRec;  // record stride between rows
   C_t<T> W[21], y[6];
 #pragma unroll
   for (int i = 0; i < 21; i++) W[i] = mk<T>(0, 0);
@@ -269,24 +339,22 @@ __global__ void __launch_bounds__(128) k_line_sweep(LevelView<T> L, int pa, int 
     W[WI(i, i)] = mk<T>(1, 0);  // dummy leading rows
     y[i] = mk<T>(0, 0);
   }
-  // forward: rows arrive in order; arriving row r eliminates pivot r-5
+  T nxt[9];
+  load_rec9<T>(base, nxt);
+  // forward: arriving row r eliminates pivot r-5
   for (int row = 0; row < m + 5; row++) {
     if (row < m) {
-      const int s = row / 5 + 1, t = row % 5;
-      switch (t) {
-        case 0: line_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, W, y); break;
-        case 1: line_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, W, y); break;
-        case 2: line_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, W, y); break;
-        case 3: line_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, W, y); break;
-        default: line_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, W, y); break;
-      }
+#pragma unroll
+      for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(nxt[j], 0);
+      W[WI(5, 5)] = mk<T>(nxt[5], nxt[6]);
+      y[5] = mk<T>(nxt[7], nxt[8]);
+      if (row + 1 < m) load_rec9<T>(base + (long)(row + 1) * rs, nxt);  // prefetch
     } else {
 #pragma unroll
       for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
       W[WI(5, 5)] = mk<T>(1, 0);
       y[5] = mk<T>(0, 0);
     }
-    // eliminate pivot in slot 0
     const C_t<T> id = crcp<T>(W[0]);
     C_t<T> lq[6];
 #pragma unroll
@@ -299,10 +367,15 @@ __global__ void __launch_bounds__(128) k_line_sweep(LevelView<T> L, int pa, int 
     }
     const int piv = row - 5;
     if (piv >= 0) {
-      C_t<T>* o = scr + (long)piv * 6 * stride + gid;
+      T* o = base + (long)piv * rs;
+      const C_t<T> z = cmul<T>(y[0], id);
 #pragma unroll
-      for (int i = 1; i < 6; i++) o[(long)(i - 1) * stride] = lq[i];
-      o[5 * stride] = cmul<T>(y[0], id);
+      for (int i = 1; i < 6; i++) {
+        o[2 * (i - 1)] = lq[i].x;
+        o[2 * (i - 1) + 1] = lq[i].y;
+      }
+      o[10] = z.x;
+      o[11] = z.y;
     }
 #pragma unroll
     for (int i = 0; i < 5; i++) {
@@ -311,40 +384,73 @@ __global__ void __launch_bounds__(128) k_line_sweep(LevelView<T> L, int pa, int 
       y[i] = y[i + 1];
     }
   }
-  // backward: x_k = z_k - sum_i l_{k+i,k} x_{k+i}; u += x
+  // backward: x_k = z_k - sum_i l_{k+i,k} x_{k+i}
   C_t<T> xw[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) xw[i] = mk<T>(0, 0);
   for (int row = m - 1; row >= 0; row--) {
-    const C_t<T>* o = scr + (long)row * 6 * stride + gid;
-    C_t<T> x = o[5 * stride];
+    T* o = base + (long)row * rs;
+    T v[12];
 #pragma unroll
-    for (int i = 0; i < 5; i++) x = cfms<T>(x, o[(long)i * stride], xw[i]);
+    for (int i = 0; i < 12; i++) v[i] = o[i];
+    C_t<T> x = mk<T>(v[10], v[11]);
+#pragma unroll
+    for (int i = 0; i < 5; i++) x = cfms<T>(x, mk<T>(v[2 * i], v[2 * i + 1]), xw[i]);
 #pragma unroll
     for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
     xw[0] = x;
-    const int s = row / 5 + 1, t = row % 5;
-    long sl;
-    switch (t) {
-      case 0: sl = line_slot<D, 0>(L.n, L.S, ta, tb, s); break;
-      case 1: sl = line_slot<D, 1>(L.n, L.S, ta, tb, s); break;
-      case 2: sl = line_slot<D, 2>(L.n, L.S, ta, tb, s); break;
-      case 3: sl = line_slot<D, 3>(L.n, L.S, ta, tb, s); break;
-      default: sl = line_slot<D, 4>(L.n, L.S, ta, tb, s); break;
-    }
-    u[sl] = cadd<T>(u[sl], x);
+    o[10] = x.x;
+    o[11] = x.y;
   }
 }
 
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_line_apply(LevelView<T> L, int pa, int pb,
+                                                    const T* __restrict__ buf) {
+  const int rhs = blockIdx.y;
+  if (L.active && !L.active[rhs]) return;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  long l;
+  int s;
+  if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
+  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  C_t<T>* u = L.u + (long)rhs * 3 * L.S;
+  const T* base = buf + (long)rhs * g.m * g.nl * kRec;
+  const int r0 = 5 * (s - 1);
+  auto add = [&](long sl, int row) {
+    const T* o = base + ((long)row * g.nl + l) * kRec;
+    u[sl] = cadd<T>(u[sl], mk<T>(o[10], o[11]));
+  };
+  add(line_slot<D, 0>(L.n, L.S, ta, tb, s), r0);
+  if (s < g.nd) {
+    add(line_slot<D, 1>(L.n, L.S, ta, tb, s), r0 + 1);
+    add(line_slot<D, 2>(L.n, L.S, ta, tb, s), r0 + 2);
+    add(line_slot<D, 3>(L.n, L.S, ta, tb, s), r0 + 3);
+    add(line_slot<D, 4>(L.n, L.S, ta, tb, s), r0 + 4);
+  }
+}
+
+template <typename T, int D>
+static void line_sweep_d(const LevelView<T>& L, int color, T* buf, cudaStream_t st) {
+  const int pa = color & 1, pb = (color >> 1) & 1;
+  const long nl = line_count(L.n, D, color);
+  if (nl == 0) return;
+  const long items = nl * L.n[D];
+  const int m = 5 * L.n[D] - 4;
+  dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
+  k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
+  dim3 g2((unsigned)((nl + 127) / 128), L.nrhs);
+  k_line_solve<T><<<g2, 128, 0, st>>>(L.active, nl, m, buf);
+  k_line_apply<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
+}
+
+// scratch: m * lines * kRec values of T (see line_scratch_elems)
 template <typename T>
 void launch_line_sweep(const LevelView<T>& L, int d, int color, C_t<T>* scratch, cudaStream_t st) {
-  const long nl = line_count(L.n, d, color);
-  if (nl == 0) return;
-  dim3 grid((unsigned)((nl + 127) / 128), L.nrhs);
-  const int pa = color & 1, pb = (color >> 1) & 1;
-  if (d == 0) k_line_sweep<T, 0><<<grid, 128, 0, st>>>(L, pa, pb, scratch);
-  else if (d == 1) k_line_sweep<T, 1><<<grid, 128, 0, st>>>(L, pa, pb, scratch);
-  else k_line_sweep<T, 2><<<grid, 128, 0, st>>>(L, pa, pb, scratch);
+  T* buf = reinterpret_cast<T*>(scratch);
+  if (d == 0) line_sweep_d<T, 0>(L, color, buf, st);
+  else if (d == 1) line_sweep_d<T, 1>(L, color, buf, st);
+  else line_sweep_d<T, 2>(L, color, buf, st);
 }
 
 // ------------------------------------------------------------ point sweep

@@ -271,7 +271,7 @@ void emmi_solver::emit_smooth(int h, int l, int iter) {
           W.active += r0;
           W.op += r0;
           launch_line_sweep<T>(W, d, col, (C_t<T>*)scratch, st);
-          launch_counter++;
+          launch_counter += 3;  // assemble, solve, apply
         }
       }
     }
@@ -518,8 +518,12 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
         for (size_t i = 0; i < gsz; i++) g32[i] = (float)g64[i];
         TRY(s->alloc((void**)&s->geo64[h][l], gsz * sizeof(double)));
         TRY(s->alloc((void**)&s->geo32[h][l], gsz * sizeof(float)));
-        CKS(cudaMemcpy(s->geo64[h][l], g64.data(), gsz * sizeof(double), cudaMemcpyHostToDevice));
-        CKS(cudaMemcpy(s->geo32[h][l], g32.data(), gsz * sizeof(float), cudaMemcpyHostToDevice));
+        // every upload goes on the solver's stream: a plain cudaMemcpy from
+        // pageable memory may return before its DMA lands, and the
+        // non-blocking stream does not wait for the legacy stream
+        CKS(cudaMemcpyAsync(s->geo64[h][l], g64.data(), gsz * sizeof(double), cudaMemcpyHostToDevice, s->st));
+        CKS(cudaMemcpyAsync(s->geo32[h][l], g32.data(), gsz * sizeof(float), cudaMemcpyHostToDevice, s->st));
+        CKS(cudaStreamSynchronize(s->st));
       }
     }
   }
@@ -542,9 +546,10 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     TRY(s->alloc((void**)&s->d_wmu32, s->nrhs * sizeof(float)));
     TRY(s->alloc((void**)&s->d_norm, s->nrhs * sizeof(double)));
     TRY(s->alloc((void**)&s->d_norm64, s->nrhs * sizeof(double)));
-    CKS(cudaMemcpy(s->d_op, op.data(), s->nrhs * sizeof(int), cudaMemcpyHostToDevice));
-    CKS(cudaMemcpy(s->d_wmu64, w64.data(), s->nrhs * sizeof(double), cudaMemcpyHostToDevice));
-    CKS(cudaMemcpy(s->d_wmu32, w32.data(), s->nrhs * sizeof(float), cudaMemcpyHostToDevice));
+    CKS(cudaMemcpyAsync(s->d_op, op.data(), s->nrhs * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    CKS(cudaMemcpyAsync(s->d_wmu64, w64.data(), s->nrhs * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CKS(cudaMemcpyAsync(s->d_wmu32, w32.data(), s->nrhs * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    CKS(cudaStreamSynchronize(s->st));
     s->h_active.assign(s->nrhs, 1);
     s->h_refine.assign(s->nrhs, 0);
   }
@@ -554,7 +559,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     const long nc0 = s->hier[0][0].ncell;
     float* raw = nullptr;
     TRY(s->alloc((void**)&raw, (size_t)s->nop * 4 * nc0 * sizeof(float)));
-    CKS(cudaMemcpy(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float), cudaMemcpyHostToDevice));
+    CKS(cudaMemcpyAsync(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float), cudaMemcpyHostToDevice, s->st));
     s->raw_cells = raw;
     // survey grids in float as emf_t holds them (regrid_init_free.c:21-34)
     {
@@ -579,15 +584,16 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
         }
       }
       TRY(s->alloc((void**)&s->sgeo, sg.size() * sizeof(float)));
-      CKS(cudaMemcpy(s->sgeo, sg.data(), sg.size() * sizeof(float), cudaMemcpyHostToDevice));
+      CKS(cudaMemcpyAsync(s->sgeo, sg.data(), sg.size() * sizeof(float), cudaMemcpyHostToDevice, s->st));
       std::vector<float> rw(s->nop, 0.f);
       if (P->rho_water)
         for (int o = 0; o < s->nop; o++) rw[o] = P->rho_water[o];
       TRY(s->alloc((void**)&s->d_rho_water, s->nop * sizeof(float)));
-      CKS(cudaMemcpy(s->d_rho_water, rw.data(), s->nop * sizeof(float), cudaMemcpyHostToDevice));
+      CKS(cudaMemcpyAsync(s->d_rho_water, rw.data(), s->nop * sizeof(float), cudaMemcpyHostToDevice, s->st));
       s->h_omega.assign(P->omega, P->omega + s->nrhs);
       TRY(s->alloc((void**)&s->d_omega, s->nrhs * sizeof(float)));
-      CKS(cudaMemcpy(s->d_omega, P->omega, s->nrhs * sizeof(float), cudaMemcpyHostToDevice));
+      CKS(cudaMemcpyAsync(s->d_omega, P->omega, s->nrhs * sizeof(float), cudaMemcpyHostToDevice, s->st));
+      CKS(cudaStreamSynchronize(s->st));
       s->h_op.resize(s->nrhs);
       for (int r = 0; r < s->nrhs; r++) s->h_op[r] = P->op ? P->op[r] : r;
     }
@@ -1035,7 +1041,7 @@ int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int
   cudaEventElapsedTime(&t, s->ev0, s->ev1);
   const double c = mixed ? 8.0 : 16.0;
   if (ms) *ms = t / reps;
-  if (launches) *launches = 4 * ((s->nrhs + s->chunk - 1) / s->chunk);
+  if (launches) *launches = 12 * ((s->nrhs + s->chunk - 1) / s->chunk);
   if (bytes) *bytes = (double)s->hier[0][0].S * (9 * c + 12) * s->nrhs;
   return EMMI_OK;
 }

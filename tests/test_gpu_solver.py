@@ -127,9 +127,10 @@ def test_batch_of_rhs_equals_individual_solves(golden):
                       options=G.Options(precision=G.PREC_MIXED, ncycle=80, tol=1e-8))
         x1, h1, st1 = s1.solve(bs[r:r + 1])
         assert stb[r]["status"] == "ok"
-        # identical arithmetic per RHS: the batch must not couple RHS
-        assert np.array_equal(xb[r], x1[0])
-        assert stb[r]["cycles"] == st1[0]["cycles"]
+        # same arithmetic per RHS: the batch must not couple RHS (norms are
+        # atomic sums, so refinement points may shift by a cycle)
+        assert rel_err(xb[r], x1[0], below_sea_mask(n, g["x3"])) < 1e-6
+        assert abs(stb[r]["cycles"] - st1[0]["cycles"]) <= 1
 
 
 @gpu
