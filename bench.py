@@ -296,13 +296,14 @@ def main():
 
     # roofline of the dominant kernel (level-0 line relaxation)
     ms, nl, by = solver.time_smoother(0, reps=5)
+    ms_dir = [round(ms, 4)] + [round(solver.time_smoother(d, reps=3)[0], 4) for d in (1, 2)]
     peak, peak_kind = peaks()
     achieved = by / (ms * 1e-3) / 1e9
     traffic = ncu_traffic()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "kernel": "k_line_sweep<float,0> (level 0, 4 colours, 25 RHS)",
-            "ms_per_sweep": round(ms, 4), "launches_per_sweep": nl,
+            "kernel": "line sweep along x: k_line_assemble/k_line_solve/k_line_apply<float> (level 0, 4 colours, 25 RHS)",
+            "ms_per_sweep": round(ms, 4), "ms_per_sweep_xyz": ms_dir, "launches_per_sweep": nl,
             "algorithmic_bytes_per_launch": by / nl, "peak_kind": peak_kind}
     solver.close()
 
