@@ -620,24 +620,26 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
         floor = 1e-4 * std::max(1.0, 2.0 * 3.14159265358979323846 / (double)wmin);
       }
       s->opt.sigma_floor = floor;
-      double* tmp[2] = {nullptr, nullptr};
-      TRY(s->alloc((void**)&tmp[0], (size_t)s->nop * 4 * nc0 * sizeof(double)));
-      TRY(s->alloc((void**)&tmp[1], (size_t)s->nop * 4 * nc0 * sizeof(double)));
+      // base: level-0 floored cells in FP64, kept intact for every
+      // hierarchy; ping/pong: the coarse levels of the current hierarchy
+      double *base = nullptr, *pp[2] = {nullptr, nullptr};
+      TRY(s->alloc((void**)&base, (size_t)s->nop * 4 * nc0 * sizeof(double)));
+      TRY(s->alloc((void**)&pp[0], (size_t)s->nop * 4 * nc0 * sizeof(double)));
+      TRY(s->alloc((void**)&pp[1], (size_t)s->nop * 4 * nc0 * sizeof(double)));
       TRY(s->alloc((void**)&s->cells32[0][0], (size_t)s->nop * 4 * nc0 * sizeof(float)));
       k_weight_cells<<<g0, 256, 0, s->st>>>(raw, s->geo64[0][0], s->gstride, s->gmax1, s->n[0],
-                                            s->n[1], s->n[2], floor, tmp[0], s->cells32[0][0]);
+                                            s->n[1], s->n[2], floor, base, s->cells32[0][0]);
       for (int h = 1; h < 3; h++) s->cells32[h][0] = s->cells32[0][0];
       for (int h = 0; h < 3; h++) {
-        int cur = 0;
+        const double* src = base;
         for (int l = 1; l < s->lmax; l++) {
           const HLev& C = s->hier[h][l];
-          const double* src = (l == 1) ? tmp[0] : tmp[cur];
-          double* dst = (l == 1) ? tmp[1] : tmp[1 - cur];
+          double* dst = pp[l & 1];
           launch_coarsen_cells<double>(src, s->hier[h][l - 1].n, dst, C.sc, s->nop, s->st);
           TRY(s->alloc((void**)&s->cells32[h][l], (size_t)s->nop * 4 * C.ncell * sizeof(float)));
           const long nn = (long)s->nop * 4 * C.ncell;
           k_d2f<<<blocks_for(nn), 256, 0, s->st>>>(dst, s->cells32[h][l], nn);
-          cur = (l == 1) ? 1 : 1 - cur;
+          src = dst;
         }
       }
       CKS(cudaStreamSynchronize(s->st));

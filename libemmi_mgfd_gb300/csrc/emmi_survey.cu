@@ -139,27 +139,30 @@ struct ChanList {
   int ch[6];
 };
 
-// one thread per RHS; b zeroed beforehand
+// one thread per RHS over its nsrc sources in order; b zeroed beforehand
 __global__ void k_inject_sources(SGrid G0, int gstride, const int* __restrict__ op,
-                                 const float* __restrict__ src, const float* __restrict__ omega,
-                                 ChanList chs, double2* __restrict__ b, int nrhs) {
+                                 const float* __restrict__ src, int nsrc,
+                                 const float* __restrict__ omega, ChanList chs,
+                                 double2* __restrict__ b, int nrhs) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrhs) return;
   SGrid G = G0;
   G.g = G0.g + (long)op[r] * gstride;
-  const float* sr = src + 5 * r;
-  zd F[3] = {{0, 0}, {0, 0}, {0, 0}};
-  const zd one = {1.0, 0.0};  // src_fd = 1 (inject_extract.c:33)
-  for (int ic = 0; ic < chs.n; ic++)
-    if (chs.ch[ic] <= 2) rotate_in(chs.ch[ic], sr[3], sr[4], one, F);
   const long S = (long)(G.n[0] + 1) * (G.n[1] + 1) * (G.n[2] + 1);
   double2* y = b + (long)r * 3 * S;
   // I*omega (complex float) * mu0 * F / vol (inject_extract.c:66)
   const zd iw = {0.0 * kMu0, (double)omega[r] * kMu0};
-  for (int c = 0; c < 3; c++) {
-    const Tri t = trilin(G, c == 0, c == 1, c == 2, sr[0], sr[1], sr[2]);
-    const zd v = zdiv_real(zmul(iw, F[c]), (double)t.vol);
-    scatter8(G.n, c, t, v, y);
+  for (int is = 0; is < nsrc; is++) {
+    const float* sr = src + 5 * ((long)r * nsrc + is);
+    zd F[3] = {{0, 0}, {0, 0}, {0, 0}};
+    const zd one = {1.0, 0.0};  // src_fd = 1 (inject_extract.c:33)
+    for (int ic = 0; ic < chs.n; ic++)
+      if (chs.ch[ic] <= 2) rotate_in(chs.ch[ic], sr[3], sr[4], one, F);
+    for (int c = 0; c < 3; c++) {
+      const Tri t = trilin(G, c == 0, c == 1, c == 2, sr[0], sr[1], sr[2]);
+      const zd v = zdiv_real(zmul(iw, F[c]), (double)t.vol);
+      scatter8(G.n, c, t, v, y);
+    }
   }
 }
 
@@ -451,19 +454,24 @@ SGrid sgrid_of(const emmi_solver* s) {
 
 extern "C" {
 
-int emmi_inject_sources_dev(emmi_solver* s, const float* src_dev, int nch, const int* ch,
-                            double* b_dev) {
-  if (!s || !src_dev || !b_dev || nch < 1 || nch > 6 || !ch) {
+int emmi_inject_sources_multi_dev(emmi_solver* s, const float* src_dev, int nsrc, int nch,
+                                  const int* ch, double* b_dev) {
+  if (!s || !src_dev || !b_dev || nch < 1 || nch > 6 || !ch || nsrc < 0) {
     set_err("emmi_inject_sources_dev: bad argument");
     return EMMI_EINVAL;
   }
   const long S = s->hier[0][0].S;
   CK(cudaMemsetAsync(b_dev, 0, (size_t)3 * S * s->nrhs * sizeof(double2), s->st));
   k_inject_sources<<<nblk(s->nrhs, 64), 64, 0, s->st>>>(sgrid_of(s), s->gstride, s->d_op, src_dev,
-                                                        s->d_omega, make_chans(nch, ch),
+                                                        nsrc, s->d_omega, make_chans(nch, ch),
                                                         (double2*)b_dev, s->nrhs);
   CK(cudaGetLastError());
   return EMMI_OK;
+}
+
+int emmi_inject_sources_dev(emmi_solver* s, const float* src_dev, int nch, const int* ch,
+                            double* b_dev) {
+  return emmi_inject_sources_multi_dev(s, src_dev, 1, nch, ch, b_dev);
 }
 
 int emmi_inject_adjoint_dev(emmi_solver* s, const float* rec_dev, int nrec, int nch, const int* ch,

@@ -35,19 +35,29 @@ def _solver(g, nrhs=1, **opt):
                     options=G.Options(**opt))
 
 
-def receiver_parity(d, dref, nch, floor=1e-3):
+def receiver_parity(d, dref, chans, floor=1e-3):
+    """Worst amplitude error (relative to the channel's scale) and phase error
+    (degrees) over receivers.  A channel's scale is its largest amplitude but
+    at least `floor` times the largest amplitude of any channel of the same
+    kind (E or H): channels that vanish by symmetry (Ey, Hx on the inline of
+    a 1D model) hold only roundoff, which has no meaningful relative error.
+    Phase is compared where the amplitude exceeds `floor` times the scale."""
+    nch = len(chans)
     d = np.asarray(d).reshape(nch, -1)
     dref = np.asarray(dref).reshape(nch, -1)
+    kind_max = {}
+    for c, nm in enumerate(chans):
+        kind_max[nm[0]] = max(kind_max.get(nm[0], 0.0), float(np.abs(dref[c]).max()))
     worst_amp, worst_ph = 0.0, 0.0
-    for c in range(nch):
-        m = np.abs(dref[c]).max()
-        if m == 0:
+    for c, nm in enumerate(chans):
+        scale = max(float(np.abs(dref[c]).max()), floor * kind_max[nm[0]])
+        if scale == 0:
             continue
-        worst_amp = max(worst_amp, np.abs(d[c] - dref[c]).max() / m)
-        sel = np.abs(dref[c]) > floor * m
+        worst_amp = max(worst_amp, float(np.abs(d[c] - dref[c]).max()) / scale)
+        sel = np.abs(dref[c]) > floor * scale
         if sel.any():
             ph = np.degrees(np.abs(np.angle(d[c][sel] / dref[c][sel])))
-            worst_ph = max(worst_ph, ph.max())
+            worst_ph = max(worst_ph, float(ph.max()))
     return worst_amp, worst_ph
 
 
@@ -85,14 +95,15 @@ def test_fp64_v_w_cycles_match_oracle(golden, cycleopt, ncyc):
 @pytest.mark.parametrize("name", ["tiny_layered", "tiny_aniso"])
 def test_converged_receivers_match_reference(golden, name, prec):
     g = golden(name)
-    s = _solver(g, precision=prec, ncycle=80, tol=1e-8)
+    # the fixture was solved by the reference to 1e-10; solve to the same
+    s = _solver(g, precision=prec, ncycle=120, tol=1e-10)
     x, h, st = s.solve(g["b_f0"][None])
     assert st[0]["status"] == "ok", st
-    assert st[0]["rel"] <= 1e-8
+    assert st[0]["rel"] <= 1e-10
     ch = str(g["chrec"]).split(",")
     rec = g["srcrec"][5:].reshape(-1, 5)
     d = O.extract_emf_data(_grid(g), rec, ch, x[0], h[0])
-    amp, ph = receiver_parity(d, g["dcal"], len(ch))
+    amp, ph = receiver_parity(d, g["dcal"], ch)
     assert amp < 1e-4, amp
     assert ph < 0.05, ph
     # the converged fields themselves, below the sea surface and H
@@ -119,12 +130,14 @@ def test_batch_of_rhs_equals_individual_solves(golden):
     n, xx, raw, om = golden_level(g)
     bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"], g["badj_f0"]])
     oms = np.array([om, om, 0.5 * om, 0.5 * om], np.float32)
+    # the default air floor depends on the batch's lowest frequency: pin it
+    opt = dict(precision=G.PREC_MIXED, ncycle=80, tol=1e-8, sigma_floor=2e-4)
     s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms, op=np.zeros(4, np.int32),
-                 options=G.Options(precision=G.PREC_MIXED, ncycle=80, tol=1e-8))
+                 options=G.Options(**opt))
     xb, hb, stb = s.solve(bs)
     for r in range(4):
         s1 = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms[r:r + 1],
-                      options=G.Options(precision=G.PREC_MIXED, ncycle=80, tol=1e-8))
+                      options=G.Options(**opt))
         x1, h1, st1 = s1.solve(bs[r:r + 1])
         assert stb[r]["status"] == "ok"
         # same arithmetic per RHS: the batch must not couple RHS (norms are
@@ -149,9 +162,18 @@ def test_config1_64_receivers_match_reference(golden):
     ch = str(g["chrec"]).split(",")
     rec = g["srcrec"][5:].reshape(-1, 5)
     d = O.extract_emf_data(_grid(g), rec, ch, x[0], h[0])
-    amp, ph = receiver_parity(d, g["dcal"], len(ch))
+    amp, ph = receiver_parity(d, g["dcal"], ch)
     assert amp < 1e-4, amp
     assert ph < 0.05, ph
+    # both against an FP64 solve to 1e-12 (the error of each is stated)
+    s64 = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], np.array([om], np.float32),
+                   options=G.Options(precision=G.PREC_FP64, ncycle=100, tol=1e-12))
+    x64, h64, st64 = s64.solve(b[None])
+    d64 = O.extract_emf_data(_grid(g), rec, ch, x64[0], h64[0])
+    ours, _ = receiver_parity(d, d64, ch)
+    ref, _ = receiver_parity(g["dcal"], d64, ch)
+    print(f"receiver error vs FP64 1e-12 solve: ours {ours:.2e}, reference {ref:.2e}")
+    assert ours < 1e-4 and ref < 1e-4
 
 
 @gpu

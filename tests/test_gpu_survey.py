@@ -163,15 +163,14 @@ def test_modelling_batch_end_to_end(golden):
     from libemmi_mgfd_gb300 import gpu as G
     n, x, raw, om = golden_level(g)
     s = G.Solver(n, *[v.astype(np.float32) for v in x], raw[None], np.array([om], np.float32),
-                 options=G.Options(precision=G.PREC_MIXED, ncycle=60, tol=1e-8),
+                 options=G.Options(precision=G.PREC_MIXED, ncycle=120, tol=1e-10),
                  rho_water=float(g["rho_water"][0]))
     rec = g["srcrec"][5:].reshape(-1, 5)
     ch = str(g["chrec"]).split(",")
     d, st, (h2d, d2h) = s.modelling(g["srcrec"][:5][None], rec, chsrc=str(g["chsrc"]).split(","),
                                     chrec=ch)
     assert st[0]["status"] == "ok"
-    ref = g["dcal"].reshape(len(ch), -1)
-    for c in range(len(ch)):
-        m = np.abs(ref[c]).max()
-        assert np.abs(d[0, c] - ref[c]).max() / m < 1e-4
+    from test_gpu_solver import receiver_parity
+    amp, ph = receiver_parity(d[0], g["dcal"], ch)
+    assert amp < 1e-4 and ph < 0.05, (amp, ph)
     assert h2d == 5 * 4 + rec.size * 4 and d2h == d.nbytes
