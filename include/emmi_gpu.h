@@ -65,8 +65,8 @@ typedef struct {
   int precision;    /* EMMI_PREC_*                                         */
   double sigma_floor; /* MIXED: conductivity floor (S/m) inside the complex64
                          preconditioner only; the FP64 residual keeps the true
-                         operator.  <=0 selects 1e-4 * max(1, 2*pi/omega).  */
-  int refine_every; /* MIXED: FP64 refinement at least every k cycles (3)  */
+                         operator.  <=0 selects 1e-5 * max(1, 2*pi/omega).  */
+  int refine_every; /* MIXED: FP64 refinement at least every k cycles (4)  */
   int use_graphs;   /* capture the cycle into CUDA graphs (1)              */
   int verb;         /* print "icycle=%d rnorm=%e" like gmg.c:1627          */
 } emmi_options;

@@ -24,6 +24,8 @@ GPU_SOURCES = ["emmi_kernels.cu", "emmi_solver.cu", "emmi_survey.cu", "emmi_drop
 HOST_SOURCES = ["emmi_host.c"]
 GPU_LIB = os.path.join(HERE, "libemmi_gpu.so")
 HOST_LIB = os.path.join(HERE, "libemmi_host.so")
+MAIN_SOURCES = ["emmi_main.c", "emmi_params.c", "emmi_host.c"]
+MAIN_BIN = os.path.join(HERE, "emmi_main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
               "--expt-relaxed-constexpr"]
@@ -74,6 +76,11 @@ def build(force: bool = False, verbose: bool = False) -> None:
     if hsrc and (force or _stale(HOST_LIB, hsrc + headers)):
         _run(["gcc", "-O2", "-fPIC", "-std=gnu99", "-shared", "-I" + INCLUDE, "-o", HOST_LIB]
              + hsrc + ["-lm"])
+    # the reference's modelling command line on the GPU path
+    msrc = [os.path.join(CSRC, f) for f in MAIN_SOURCES]
+    if force or _stale(MAIN_BIN, msrc + headers + [GPU_LIB]):
+        _run(["gcc", "-O2", "-std=gnu99", "-I" + INCLUDE, "-o", MAIN_BIN] + msrc
+             + ["-L" + HERE, "-lemmi_gpu", "-Wl,-rpath,$ORIGIN", "-lm"])
 
 
 if __name__ == "__main__":

@@ -48,6 +48,10 @@ template <typename T> __device__ __forceinline__ C_t<T> crcp(C_t<T> z) {
   return mk<T>(ldexp(zx * inv, -e), ldexp(-zy * inv, -e));
 }
 
+// read-only (non-coherent) loads: the data a kernel only reads during its
+// launch; lets loads move past the kernel's own stores
+template <typename T> __device__ __forceinline__ T ldro(const T* p) { return __ldg(p); }
+
 // ---------------------------------------------------------------- views
 // One multigrid level of a batch, in working precision T.
 template <typename T> struct LevelView {
@@ -142,15 +146,15 @@ __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const 
   const long c10 = c11 - cs[q];                                     // (b, g-1)
   const long c01 = c11 - cs[p];                                     // (b-1, g)
   const long c00 = c01 - cs[q];                                     // (b-1, g-1)
-  const T s = T(0.25) * (((sigC[c00] + sigC[c01]) + sigC[c10]) + sigC[c11]);
-  const T i00 = imu[c00], i01 = imu[c01], i10 = imu[c10], i11 = imu[c11];
+  const T s = T(0.25) * (((ldro(sigC + c00) + ldro(sigC + c01)) + ldro(sigC + c10)) + ldro(sigC + c11));
+  const T i00 = ldro(imu + c00), i01 = ldro(imu + c01), i10 = ldro(imu + c10), i11 = ldro(imu + c11);
   const T m1 = T(0.5) * (i11 + i10);  // H_q face at p=b
   const T m2 = T(0.5) * (i01 + i00);  // H_q face at p=b-1
   const T m3 = T(0.5) * (i11 + i01);  // H_p face at q=g
   const T m4 = T(0.5) * (i10 + i00);  // H_p face at q=g-1
-  const T dc = G.ds(C)[a];
-  const T dpp = G.ds(p)[b], dpm = G.ds(p)[b - 1];
-  const T dqp = G.ds(q)[g], dqm = G.ds(q)[g - 1];
+  const T dc = ldro(G.ds(C) + a);
+  const T dpp = ldro(G.ds(p) + b), dpm = ldro(G.ds(p) + b - 1);
+  const T dqp = ldro(G.ds(q) + g), dqm = ldro(G.ds(q) + g - 1);
   const T kpp = m1 / (dpp * dpp), kpm = m2 / (dpm * dpm);
   const T kqp = m3 / (dqp * dqp), kqm = m4 / (dqm * dqm);
   e.dre = (kpp + kpm) + (kqp + kqm);

@@ -104,13 +104,15 @@ __device__ __forceinline__ C_t<T> apply_row(const LevelView<T>& L, const C_t<T>*
                                             const T* __restrict__ cells, const Geo<T>& G, T wmu,
                                             const int P[3], long s, const long ss[3],
                                             EdgeCoef<T>& e) {
+  // u, cells and geometry are not written by any thread while a residual,
+  // an assembly or a same-colour block sweep reads them: read-only loads
   edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
-  const C_t<T> uc = u[(long)C * L.S + s];
+  const C_t<T> uc = ldro(u + (long)C * L.S + s);
   T ar = e.dre * uc.x - e.dim * uc.y;
   T ai = e.dre * uc.y + e.dim * uc.x;
 #pragma unroll
   for (int k = 0; k < 12; k++) {
-    const C_t<T> v = u[s + nbr_slot_delta<C>(k, ss, L.S)];
+    const C_t<T> v = ldro(u + s + nbr_slot_delta<C>(k, ss, L.S));
     ar += e.c[k] * v.x;
     ai += e.c[k] * v.y;
   }
@@ -205,8 +207,43 @@ void launch_norm(const C_t<T>* v, long n3s, int nrhs, const int* active, double*
 // Record of one row, T-typed: [0..4] band, [5,6] diagonal, [7,8] residual;
 // after the forward pass [0..9] = l_1..l_5 (complex), [10,11] = z; after the
 // backward pass [10,11] = the correction x.
+// Records are stored as 16-byte planes, [row][plane][line]: plane q of a row
+// holds record values [q*L, q*L+L) with L = 16/sizeof(T) (3 planes for float,
+// 6 for double), so one warp-wide 16-byte access of consecutive lines reads
+// or writes 512 contiguous bytes.
 #define WI(i, j) ((i) * ((i) + 1) / 2 + (j))
 constexpr int kRec = 12;
+
+__device__ __forceinline__ float4 pack16(const float* v) { return make_float4(v[0], v[1], v[2], v[3]); }
+__device__ __forceinline__ double2 pack16(const double* v) { return make_double2(v[0], v[1]); }
+__device__ __forceinline__ void unpack16(const float4& w, float* v) {
+  v[0] = w.x; v[1] = w.y; v[2] = w.z; v[3] = w.w;
+}
+__device__ __forceinline__ void unpack16(const double2& w, double* v) { v[0] = w.x; v[1] = w.y; }
+
+template <typename T> struct Vec16 { using V = float4; };
+template <> struct Vec16<double> { using V = double2; };
+template <typename T> constexpr int kLanes = 16 / (int)sizeof(T);
+template <typename T> constexpr int kPlanes = kRec / kLanes<T>;
+
+// p: plane 0 of one (row, line); ps: distance between planes (= lines)
+template <typename T>
+__device__ __forceinline__ void rec_put(typename Vec16<T>::V* p, long ps, const T (&v)[kRec]) {
+#pragma unroll
+  for (int q = 0; q < kPlanes<T>; q++) p[q * ps] = pack16(v + q * kLanes<T>);
+}
+template <typename T>
+__device__ __forceinline__ void rec_get(const typename Vec16<T>::V* p, long ps, T (&v)[kRec]) {
+#pragma unroll
+  for (int q = 0; q < kPlanes<T>; q++) unpack16(p[q * ps], v + q * kLanes<T>);
+}
+// values [10,11] (z or x) live in the last plane for both types
+template <typename T>
+__device__ __forceinline__ C_t<T> rec_get_x(const typename Vec16<T>::V* p, long ps) {
+  T v[kLanes<T>];
+  unpack16(p[(kPlanes<T> - 1) * ps], v);
+  return mk<T>(v[kLanes<T> - 2], v[kLanes<T> - 1]);
+}
 
 struct LineGeom {
   int la, lb, fa, fb;  // lines per transverse direction and first index
@@ -246,7 +283,8 @@ template <typename T, int D, int TT, int C>
 __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>* u,
                                              const C_t<T>* f, const T* cells, const Geo<T>& G,
                                              T wmu, int ta, int tb, int s, int row,
-                                             const long ss[3], T* __restrict__ rec) {
+                                             const long ss[3], typename Vec16<T>::V* rp,
+                                             long ps) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   int P[3];
   P[D] = (TT == 0) ? s - 1 : s;
@@ -267,12 +305,15 @@ __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>
   LINE_ENTRY(0) LINE_ENTRY(1) LINE_ENTRY(2) LINE_ENTRY(3) LINE_ENTRY(4) LINE_ENTRY(5)
   LINE_ENTRY(6) LINE_ENTRY(7) LINE_ENTRY(8) LINE_ENTRY(9) LINE_ENTRY(10) LINE_ENTRY(11)
 #undef LINE_ENTRY
+  T rec[kRec];
 #pragma unroll
   for (int i = 0; i < 5; i++) rec[i] = band[i];
   rec[5] = e.dre;
   rec[6] = e.dim;
   rec[7] = r.x;
   rec[8] = r.y;
+  rec[9] = rec[10] = rec[11] = 0;
+  rec_put<T>(rp, ps, rec);
 }
 
 template <int D, int TT>
@@ -287,7 +328,7 @@ __device__ __forceinline__ long line_slot(const int n[3], long S, int ta, int tb
 }
 
 template <typename T, int D>
-__global__ void __launch_bounds__(256) k_line_assemble(LevelView<T> L, int pa, int pb,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(LevelView<T> L, int pa, int pb,
                                                        T* __restrict__ buf) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   const int rhs = blockIdx.y;
@@ -304,33 +345,30 @@ __global__ void __launch_bounds__(256) k_line_assemble(LevelView<T> L, int pa, i
   const T* cells = L.cells + (long)op_of(L, rhs) * 4 * L.ncell;
   const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
   const T wmu = L.wmu[rhs];
-  T* base = buf + (long)rhs * g.m * g.nl * kRec;
+  using V = typename Vec16<T>::V;
+  V* base = reinterpret_cast<V*>(buf) + (long)rhs * g.m * kPlanes<T> * g.nl;
+  const long ps = g.nl;
   const int r0 = 5 * (s - 1);
-  auto rec = [&](int row) { return base + ((long)row * g.nl + l) * kRec; };
-  assemble_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0));
+  auto rec = [&](int row) { return base + (long)row * kPlanes<T> * g.nl + l; };
+  assemble_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0), ps);
   if (s < g.nd) {
-    assemble_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1));
-    assemble_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2));
-    assemble_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3));
-    assemble_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4));
+    assemble_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1), ps);
+    assemble_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2), ps);
+    assemble_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3), ps);
+    assemble_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4), ps);
   }
 }
 
 template <typename T>
-__device__ __forceinline__ void load_rec9(const T* p, T (&v)[9]) {
-#pragma unroll
-  for (int i = 0; i < 9; i++) v[i] = p[i];
-}
-
-template <typename T>
-__global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ active, long nl, int m,
-                                                    T* __restrict__ buf) {
+__global__ void __launch_bounds__(64) k_line_solve(const int* __restrict__ active, long nl, int m,
+                                                   T* __restrict__ buf) {
+  using V = typename Vec16<T>::V;
   const int rhs = blockIdx.y;
   if (active && !active[rhs]) return;
   const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (l >= nl) return;
-  T* base = buf + (long)rhs * m * nl * kRec + l * kRec;
-  const long rs = nl * kRec;  // record stride between rows
+  V* base = reinterpret_cast<V*>(buf) + (long)rhs * m * kPlanes<T> * nl + l;
+  const long rs = kPlanes<T> * nl;  // distance between rows
   C_t<T> W[21], y[6];
 #pragma unroll
   for (int i = 0; i < 21; i++) W[i] = mk<T>(0, 0);
@@ -339,8 +377,8 @@ __global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ acti
     W[WI(i, i)] = mk<T>(1, 0);  // dummy leading rows
     y[i] = mk<T>(0, 0);
   }
-  T nxt[9];
-  load_rec9<T>(base, nxt);
+  T nxt[kRec];
+  rec_get<T>(base, nl, nxt);
   // forward: arriving row r eliminates pivot r-5
   for (int row = 0; row < m + 5; row++) {
     if (row < m) {
@@ -348,7 +386,7 @@ __global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ acti
       for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(nxt[j], 0);
       W[WI(5, 5)] = mk<T>(nxt[5], nxt[6]);
       y[5] = mk<T>(nxt[7], nxt[8]);
-      if (row + 1 < m) load_rec9<T>(base + (long)(row + 1) * rs, nxt);  // prefetch
+      if (row + 1 < m) rec_get<T>(base + (long)(row + 1) * rs, nl, nxt);  // prefetch
     } else {
 #pragma unroll
       for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
@@ -367,8 +405,8 @@ __global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ acti
     }
     const int piv = row - 5;
     if (piv >= 0) {
-      T* o = base + (long)piv * rs;
       const C_t<T> z = cmul<T>(y[0], id);
+      T o[kRec];
 #pragma unroll
       for (int i = 1; i < 6; i++) {
         o[2 * (i - 1)] = lq[i].x;
@@ -376,6 +414,7 @@ __global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ acti
       }
       o[10] = z.x;
       o[11] = z.y;
+      rec_put<T>(base + (long)piv * rs, nl, o);
     }
 #pragma unroll
     for (int i = 0; i < 5; i++) {
@@ -388,19 +427,23 @@ __global__ void __launch_bounds__(128) k_line_solve(const int* __restrict__ acti
   C_t<T> xw[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) xw[i] = mk<T>(0, 0);
+  T v[kRec];
+  rec_get<T>(base + (long)(m - 1) * rs, nl, v);
   for (int row = m - 1; row >= 0; row--) {
-    T* o = base + (long)row * rs;
-    T v[12];
-#pragma unroll
-    for (int i = 0; i < 12; i++) v[i] = o[i];
+    V* o = base + (long)row * rs;
     C_t<T> x = mk<T>(v[10], v[11]);
 #pragma unroll
     for (int i = 0; i < 5; i++) x = cfms<T>(x, mk<T>(v[2 * i], v[2 * i + 1]), xw[i]);
+    T last[kLanes<T>];
+#pragma unroll
+    for (int i = 0; i < kLanes<T>; i++) last[i] = v[kRec - kLanes<T> + i];
+    if (row > 0) rec_get<T>(base + (long)(row - 1) * rs, nl, v);  // prefetch
 #pragma unroll
     for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
     xw[0] = x;
-    o[10] = x.x;
-    o[11] = x.y;
+    last[kLanes<T> - 2] = x.x;
+    last[kLanes<T> - 1] = x.y;
+    o[(kPlanes<T> - 1) * nl] = pack16(last);
   }
 }
 
@@ -414,12 +457,12 @@ __global__ void __launch_bounds__(256) k_line_apply(LevelView<T> L, int pa, int 
   int s;
   if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
   const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  using V = typename Vec16<T>::V;
   C_t<T>* u = L.u + (long)rhs * 3 * L.S;
-  const T* base = buf + (long)rhs * g.m * g.nl * kRec;
+  const V* base = reinterpret_cast<const V*>(buf) + (long)rhs * g.m * kPlanes<T> * g.nl + l;
   const int r0 = 5 * (s - 1);
   auto add = [&](long sl, int row) {
-    const T* o = base + ((long)row * g.nl + l) * kRec;
-    u[sl] = cadd<T>(u[sl], mk<T>(o[10], o[11]));
+    u[sl] = cadd<T>(u[sl], rec_get_x<T>(base + (long)row * kPlanes<T> * g.nl, g.nl));
   };
   add(line_slot<D, 0>(L.n, L.S, ta, tb, s), r0);
   if (s < g.nd) {
@@ -439,8 +482,8 @@ static void line_sweep_d(const LevelView<T>& L, int color, T* buf, cudaStream_t 
   const int m = 5 * L.n[D] - 4;
   dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
   k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
-  dim3 g2((unsigned)((nl + 127) / 128), L.nrhs);
-  k_line_solve<T><<<g2, 128, 0, st>>>(L.active, nl, m, buf);
+  dim3 g2((unsigned)((nl + 63) / 64), L.nrhs);
+  k_line_solve<T><<<g2, 64, 0, st>>>(L.active, nl, m, buf);
   k_line_apply<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
 }
 

@@ -100,7 +100,7 @@ class Options:
     isemicoarsen: int = 1
     precision: int = PREC_MIXED
     sigma_floor: float = 0.0
-    refine_every: int = 3
+    refine_every: int = 4
     use_graphs: int = 1
     verb: int = 0
 
