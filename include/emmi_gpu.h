@@ -196,6 +196,32 @@ int emmi_level_smooth(const int n[3], const double *x1, const double *x2,
                       const double *x3, const double *cells, double omega,
                       int prec, int dir, int iter, double *u, const double *f);
 
+/* ---- allocation-free line sweep --------------------------------------- */
+/* No counterpart in the reference.  The same sweep as emmi_level_smooth
+ * with dir 0..2, for callers that cannot allocate device memory: a program
+ * whose memory pool already owns the GPU's HBM, or one whose streams must not
+ * be stalled by the device-wide synchronization of cudaMalloc/cudaFree.  It
+ * allocates nothing: its scratch (the sweep's band records and the level's
+ * geometry) is one static device array of EMMI_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading this library holds until the process exits.
+ *   cells  device, [4][n3][n2][n1] volume-weighted, double for EMMI_PREC_FP64,
+ *          float for EMMI_PREC_MIXED
+ *   u, f   device, [3][(n3+1)(n2+1)(n1+1)] complex double / complex float;
+ *          u is updated in place
+ *   x1..x3 host node coordinates (n_d+1 each); stream may be NULL
+ * Levels whose sweep needs more scratch than the maximum, or with n_d
+ * outside [2, EMMI_NOALLOC_MAX_N], return EMMI_EINVAL (see emmi_last_error).
+ * The first call on a device looks up the array's address on that device;
+ * make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, calls ordered on one stream do not. */
+#define EMMI_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define EMMI_NOALLOC_MAX_N 1024
+int emmi_level_line_sweep_noalloc(const int n[3], const double *x1,
+                                  const double *x2, const double *x3,
+                                  const void *cells, double omega, int prec,
+                                  int dir, int iter, void *u, const void *f,
+                                  void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-GPU_SOURCES = ["emmi_kernels.cu", "emmi_solver.cu", "emmi_survey.cu", "emmi_dropin.cu"]
+GPU_SOURCES = ["emmi_kernels.cu", "emmi_solver.cu", "emmi_survey.cu", "emmi_dropin.cu",
+               "emmi_noalloc.cu"]
 HOST_SOURCES = ["emmi_host.c"]
 GPU_LIB = os.path.join(HERE, "libemmi_gpu.so")
 HOST_LIB = os.path.join(HERE, "libemmi_host.so")
