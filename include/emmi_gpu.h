@@ -69,6 +69,9 @@ typedef struct {
   int refine_every; /* MIXED: FP64 refinement at least every k cycles (4)  */
   int use_graphs;   /* capture the cycle into CUDA graphs (1)              */
   int verb;         /* print "icycle=%d rnorm=%e" like gmg.c:1627          */
+  int krylov;       /* MIXED: 0 = stationary FP64 refinement of complex64
+                       cycles; k > 0 = FP64 FGMRES(k) (k <= 12) with one
+                       complex64 cycle as its preconditioner (0)           */
 } emmi_options;
 
 typedef struct {
@@ -77,6 +80,8 @@ typedef struct {
   double rnorm0;    /* |b_vol|                                            */
   double rnorm;     /* final |b_vol - A x| (FP64)                         */
   int refinements;  /* MIXED: FP64 residual evaluations                   */
+  int fallback;     /* 1 if the learned correction was switched off for
+                       this RHS because its residual stalled               */
 } emmi_rhs_stats;
 
 typedef struct emmi_solver emmi_solver;
@@ -117,6 +122,36 @@ void emmi_solver_destroy(emmi_solver *s);
 
 const char *emmi_last_error(void);
 
+/* ---- learned correction (no counterpart in the reference) -------------- */
+/* A small linear 3x3x3 convolutional network (8 -> 8 -> 8 channels, bf16
+ * tensor-core forward, 2 x 1728 fp32 weights [layer][tap][cin][cout], tap =
+ * (dk+1)*9+(dj+1)*3+(di+1)) that corrects the level-0 complex64 iterate after
+ * every cycle of a MIXED solver: u += N(D^-1 (f - A u)) on unknown edges.
+ * Training minimises sum_b |r_b - A N(D^-1 r_b)|^2 / |r_b|^2 over residual
+ * samples r_b of plain cycles.  A RHS whose FP64 residual does not halve
+ * between refinements (restarts with krylov) with the correction on falls
+ * back to plain cycles (emmi_rhs_stats.fallback). */
+/* Solve b (as emmi_solver_solve, solution discarded) with plain cycles and
+ * keep the level-0 residual after each of the first per_rhs cycles of every
+ * RHS as training samples (stationary MIXED solvers). */
+int emmi_learned_collect(emmi_solver *s, const double *b, int device,
+                         int per_rhs, emmi_rhs_stats *stats);
+/* Add ns samples r ([ns][3*S] complex float, host) of the operators of RHS
+ * rhs[k] to the training set. */
+int emmi_learned_add_samples(emmi_solver *s, int ns, const float *r,
+                             const int *rhs);
+int emmi_learned_samples(const emmi_solver *s);
+/* steps full-batch Adam steps (rate lr) on the GPU from W (in/out); loss
+ * (optional, [steps]): mean normalised loss before each step. */
+int emmi_learned_train(emmi_solver *s, int steps, float lr, float *W,
+                       float *loss);
+/* loss (mean over samples) and dLoss_sum/dW ([2][1728], sum over samples of
+ * the normalised losses) at W, without updating */
+int emmi_learned_grad(emmi_solver *s, const float *W, float *loss,
+                      float *grad);
+/* use W in the following solves; W = NULL switches the correction off */
+int emmi_learned_set(emmi_solver *s, const float *W);
+
 /* ---- survey: injection, extraction, gradient (src/inject_extract.c,
  *      src/build_gradient.c) ------------------------------------------- */
 /* channel codes: 0..2 = Ex,Ey,Ez ; 3..5 = Hx,Hy,Hz */
@@ -139,7 +174,8 @@ int emmi_modelling_batch(emmi_solver *s, const emmi_survey *sv, float *dcal,
                          emmi_rhs_stats *stats, size_t *h2d, size_t *d2h);
 
 /* Device-resident variants used by the batch path and the drop-in layer.
- * All pointers are device pointers; fields [nrhs][3*S] complex double. */
+ * Data pointers are device pointers (fields [nrhs][3*S] complex double);
+ * the channel lists ch (codes 0..5, at most 6) are host arrays. */
 int emmi_inject_sources_dev(emmi_solver *s, const float *src_dev, int nch,
                             const int *ch, double *b_dev);
 /* adjoint sources from receiver residuals dres_dev [nrhs][nch][nrec]

@@ -184,4 +184,25 @@ __device__ __forceinline__ long nbr_slot_delta(int k, const long ss[3], long S) 
   return (long)o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
 }
 
+// (A u) of the edge equation of component C at slot s, and its coefficients
+template <typename T, int C>
+__device__ __forceinline__ C_t<T> apply_row(const LevelView<T>& L, const C_t<T>* __restrict__ u,
+                                            const T* __restrict__ cells, const Geo<T>& G, T wmu,
+                                            const int P[3], long s, const long ss[3],
+                                            EdgeCoef<T>& e) {
+  // u, cells and geometry are not written by any thread while a residual,
+  // an assembly or a same-colour block sweep reads them: read-only loads
+  edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
+  const C_t<T> uc = ldro(u + (long)C * L.S + s);
+  T ar = e.dre * uc.x - e.dim * uc.y;
+  T ai = e.dre * uc.y + e.dim * uc.x;
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const C_t<T> v = ldro(u + s + nbr_slot_delta<C>(k, ss, L.S));
+    ar += e.c[k] * v.x;
+    ai += e.c[k] * v.y;
+  }
+  return mk<T>(ar, ai);
+}
+
 }  // namespace emmi

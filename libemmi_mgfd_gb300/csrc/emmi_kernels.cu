@@ -60,7 +60,6 @@ __host__ __device__ constexpr int line_off(int d, int t, int k) {
   return pos < 0 ? 127 : pos - row;
 }
 
-void init_line_tables() {}
 
 long line_count(const int n[3], int d, int color) {
   const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
@@ -99,26 +98,6 @@ __device__ __forceinline__ void block_add(double v, double* dst) {
 }
 
 // ------------------------------------------------------------ residual
-template <typename T, int C>
-__device__ __forceinline__ C_t<T> apply_row(const LevelView<T>& L, const C_t<T>* __restrict__ u,
-                                            const T* __restrict__ cells, const Geo<T>& G, T wmu,
-                                            const int P[3], long s, const long ss[3],
-                                            EdgeCoef<T>& e) {
-  // u, cells and geometry are not written by any thread while a residual,
-  // an assembly or a same-colour block sweep reads them: read-only loads
-  edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
-  const C_t<T> uc = ldro(u + (long)C * L.S + s);
-  T ar = e.dre * uc.x - e.dim * uc.y;
-  T ai = e.dre * uc.y + e.dim * uc.x;
-#pragma unroll
-  for (int k = 0; k < 12; k++) {
-    const C_t<T> v = ldro(u + s + nbr_slot_delta<C>(k, ss, L.S));
-    ar += e.c[k] * v.x;
-    ai += e.c[k] * v.y;
-  }
-  return mk<T>(ar, ai);
-}
-
 template <int C>
 __device__ __forceinline__ bool is_unknown(const int n[3], const int P[3]) {
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
@@ -130,7 +109,7 @@ __device__ __forceinline__ double residual_comp(const LevelView<T>& L, const C_t
                                                 const C_t<T>* f, const T* cells, const Geo<T>& G,
                                                 T wmu, const int P[3], long s, const long ss[3],
                                                 C_t<TO>* rout) {
-  C_t<T> r = f[(long)C * L.S + s];
+  C_t<T> r = f ? f[(long)C * L.S + s] : mk<T>(0, 0);  // f null: r = -A u
   if (is_unknown<C>(L.n, P)) {
     EdgeCoef<T> e;
     const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, s, ss, e);
@@ -152,7 +131,7 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
     const int P[3] = {(int)(s % n0), (int)((s / n0) % n1), (int)(s / ((long)n0 * n1))};
     const long ss[3] = {1, (long)n0, (long)n0 * n1};
     const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
-    const C_t<T>* f = L.f + (long)rhs * 3 * L.S;
+    const C_t<T>* f = L.f ? L.f + (long)rhs * 3 * L.S : nullptr;
     const T* cells = L.cells + (long)op_of(L, rhs) * 4 * L.ncell;
     const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
     const T wmu = L.wmu[rhs];
@@ -327,9 +306,12 @@ __device__ __forceinline__ long line_slot(const int n[3], long S, int ta, int tb
   return (long)C * S + slot_id(n, P[0], P[1], P[2]);
 }
 
+// one thread per (line, node) and its five rows: y and z lines, whose
+// neighbouring lines are neighbouring slots
 template <typename T, int D>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(LevelView<T> L, int pa, int pb,
-                                                       T* __restrict__ buf) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(LevelView<T> L,
+                                                                              int pa, int pb,
+                                                                              T* __restrict__ buf) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   const int rhs = blockIdx.y;
   if (L.active && !L.active[rhs]) return;
@@ -359,16 +341,91 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(L
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(64) k_line_solve(const int* __restrict__ active, long nl, int m,
-                                                   T* __restrict__ buf) {
+// one thread per (row type, line, node), row type slowest: x lines, where a
+// thread owning all five rows of a node holds too many registers for the
+// latency of its scattered record stores (a warp shares one row type)
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_line_assemble_rows(LevelView<T> L, int pa, int pb,
+                                                            T* __restrict__ buf) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  const int rhs = blockIdx.y;
+  if (L.active && !L.active[rhs]) return;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  const long items = g.nl * g.nd;
+  const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int rt = (int)(id / items);
+  if (rt >= 5) return;
+  long l;
+  int s;
+  if (!line_item<D>(g, id - rt * items, l, s)) return;
+  if (rt > 0 && s == g.nd) return;  // the last node carries only its E_D row
+  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
+  const long ss[3] = {1, (long)n0, (long)n0 * n1};
+  const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
+  const C_t<T>* f = L.f + (long)rhs * 3 * L.S;
+  const T* cells = L.cells + (long)op_of(L, rhs) * 4 * L.ncell;
+  const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
+  const T wmu = L.wmu[rhs];
   using V = typename Vec16<T>::V;
+  V* base = reinterpret_cast<V*>(buf) + (long)rhs * g.m * kPlanes<T> * g.nl;
+  const long ps = g.nl;
+  const int row = 5 * (s - 1) + rt;
+  V* rp = base + (long)row * kPlanes<T> * g.nl + l;
+  switch (rt) {
+    case 0: assemble_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, rp, ps); break;
+    case 1: assemble_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, rp, ps); break;
+    case 2: assemble_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, rp, ps); break;
+    case 3: assemble_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, rp, ps); break;
+    default: assemble_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, row, ss, rp, ps); break;
+  }
+}
+
+// Each thread streams its line's records through a private ring of kRing
+// rows in shared memory ([slot][plane][thread], conflict-free 16-byte
+// accesses), filled by cp.async kRing-1 rows ahead of the elimination: the
+// row-to-row dependency of the factorization no longer waits on a memory
+// round trip.
+constexpr int kRing = 6;
+constexpr int kSolveThreads = 64;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads) k_line_solve(const int* __restrict__ active,
+                                                              long nl, int m,
+                                                              T* __restrict__ buf) {
+  using V = typename Vec16<T>::V;
+  constexpr int NP = kPlanes<T>;
+  __shared__ V ring[kRing][NP][kSolveThreads];
   const int rhs = blockIdx.y;
   if (active && !active[rhs]) return;
-  const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int tid = threadIdx.x;
+  const long l = blockIdx.x * (long)blockDim.x + tid;
   if (l >= nl) return;
-  V* base = reinterpret_cast<V*>(buf) + (long)rhs * m * kPlanes<T> * nl + l;
-  const long rs = kPlanes<T> * nl;  // distance between rows
+  V* base = reinterpret_cast<V*>(buf) + (long)rhs * m * NP * nl + l;
+  const long rs = NP * nl;  // distance between rows
+  auto issue = [&](int row) {
+    const V* src = base + (long)row * rs;
+    const int slot = row % kRing;
+#pragma unroll
+    for (int q = 0; q < NP; q++) cp_async16(&ring[slot][q][tid], src + q * nl);
+  };
+  auto take = [&](int row, T (&v)[kRec]) {
+    const int slot = row % kRing;
+#pragma unroll
+    for (int q = 0; q < NP; q++) unpack16(ring[slot][q][tid], v + q * kLanes<T>);
+  };
   C_t<T> W[21], y[6];
 #pragma unroll
   for (int i = 0; i < 21; i++) W[i] = mk<T>(0, 0);
@@ -377,16 +434,22 @@ __global__ void __launch_bounds__(64) k_line_solve(const int* __restrict__ activ
     W[WI(i, i)] = mk<T>(1, 0);  // dummy leading rows
     y[i] = mk<T>(0, 0);
   }
-  T nxt[kRec];
-  rec_get<T>(base, nl, nxt);
+  for (int p = 0; p < kRing - 1; p++) {
+    if (p < m) issue(p);
+    cp_async_commit();
+  }
   // forward: arriving row r eliminates pivot r-5
   for (int row = 0; row < m + 5; row++) {
     if (row < m) {
+      if (row + kRing - 1 < m) issue(row + kRing - 1);
+      cp_async_commit();
+      cp_async_wait<kRing - 1>();
+      T nxt[kRec];
+      take(row, nxt);
 #pragma unroll
       for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(nxt[j], 0);
       W[WI(5, 5)] = mk<T>(nxt[5], nxt[6]);
       y[5] = mk<T>(nxt[7], nxt[8]);
-      if (row + 1 < m) rec_get<T>(base + (long)(row + 1) * rs, nl, nxt);  // prefetch
     } else {
 #pragma unroll
       for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
@@ -423,28 +486,36 @@ __global__ void __launch_bounds__(64) k_line_solve(const int* __restrict__ activ
       y[i] = y[i + 1];
     }
   }
+  cp_async_wait<0>();
+  __threadfence_block();  // the factors just stored are read back below
   // backward: x_k = z_k - sum_i l_{k+i,k} x_{k+i}
   C_t<T> xw[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) xw[i] = mk<T>(0, 0);
-  T v[kRec];
-  rec_get<T>(base + (long)(m - 1) * rs, nl, v);
+  for (int p = 0; p < kRing - 1; p++) {
+    if (m - 1 - p >= 0) issue(m - 1 - p);
+    cp_async_commit();
+  }
   for (int row = m - 1; row >= 0; row--) {
-    V* o = base + (long)row * rs;
+    if (row - (kRing - 1) >= 0) issue(row - (kRing - 1));
+    cp_async_commit();
+    cp_async_wait<kRing - 1>();
+    T v[kRec];
+    take(row, v);
     C_t<T> x = mk<T>(v[10], v[11]);
 #pragma unroll
     for (int i = 0; i < 5; i++) x = cfms<T>(x, mk<T>(v[2 * i], v[2 * i + 1]), xw[i]);
-    T last[kLanes<T>];
-#pragma unroll
-    for (int i = 0; i < kLanes<T>; i++) last[i] = v[kRec - kLanes<T> + i];
-    if (row > 0) rec_get<T>(base + (long)(row - 1) * rs, nl, v);  // prefetch
 #pragma unroll
     for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
     xw[0] = x;
+    T last[kLanes<T>];
+#pragma unroll
+    for (int i = 0; i < kLanes<T>; i++) last[i] = v[kRec - kLanes<T> + i];
     last[kLanes<T> - 2] = x.x;
     last[kLanes<T> - 1] = x.y;
-    o[(kPlanes<T> - 1) * nl] = pack16(last);
+    base[(long)row * rs + (NP - 1) * nl] = pack16(last);
   }
+  cp_async_wait<0>();
 }
 
 template <typename T, int D>
@@ -473,6 +544,323 @@ __global__ void __launch_bounds__(256) k_line_apply(LevelView<T> L, int pa, int 
   }
 }
 
+// ---------------------------------------------------------------- stored line factors
+// A line's band matrix depends on the operator only, never on the iterate.
+// The complex64 solver can therefore keep the LDL^T factors of every line
+// (one record per row: L(p+i, p) for i = 1..5 and 1/d_p, the 12 values
+// k_line_solve writes in place, as planes [row][plane][line]) and sweep with
+// a residual per row and a substitution: the same arithmetic in the same
+// order as k_line_solve, so the same result, with 8 instead of 48 bytes per
+// row written by the assembly and no complex reciprocal per row.
+
+template <typename T, int D, int TT, int C>
+__device__ __forceinline__ C_t<T> row_residual(const LevelView<T>& L, const C_t<T>* u,
+                                               const C_t<T>* f, const T* cells,
+                                               const Geo<T>& G, T wmu, int ta, int tb, int s,
+                                               const long ss[3]) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  int P[3];
+  P[D] = (TT == 0) ? s - 1 : s;
+  P[A] = ta - (TT == 1 ? 1 : 0);
+  P[B] = tb - (TT == 3 ? 1 : 0);
+  const long sl = slot_id(L.n, P[0], P[1], P[2]);
+  EdgeCoef<T> e;
+  const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
+  return csub<T>(f[(long)C * L.S + sl], au);
+}
+
+// rb[rhs][row][line] = residual of every row of one colour; y and z lines:
+// a thread per (line, node) and its five rows; x lines: a thread per
+// (row type, line, node), row type slowest
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb,
+                                                  C_t<T>* __restrict__ rb) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  const int rhs = blockIdx.y;
+  if (L.active && !L.active[rhs]) return;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  const long items = g.nl * g.nd;
+  long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int rt = 0;
+  if (D == 0) {
+    rt = (int)(id / items);
+    if (rt >= 5) return;
+    id -= rt * items;
+  }
+  long l;
+  int s;
+  if (!line_item<D>(g, id, l, s)) return;
+  if (D == 0 && rt > 0 && s == g.nd) return;
+  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
+  const long ss[3] = {1, (long)n0, (long)n0 * n1};
+  const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
+  const C_t<T>* f = L.f + (long)rhs * 3 * L.S;
+  const T* cells = L.cells + (long)op_of(L, rhs) * 4 * L.ncell;
+  const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
+  const T wmu = L.wmu[rhs];
+  C_t<T>* out = rb + (long)rhs * g.m * g.nl + l;
+  const int r0 = 5 * (s - 1);
+  auto put = [&](int row, C_t<T> v) { out[(long)row * g.nl] = v; };
+  if (D == 0) {
+    switch (rt) {
+      case 0: put(r0, row_residual<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 1: put(r0 + 1, row_residual<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 2: put(r0 + 2, row_residual<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 3: put(r0 + 3, row_residual<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      default: put(r0 + 4, row_residual<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+    }
+  } else {
+    put(r0, row_residual<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+    if (s < g.nd) {
+      put(r0 + 1, row_residual<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 2, row_residual<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 3, row_residual<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 4, row_residual<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+    }
+  }
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void cp_async_c(C_t<T>* smem, const C_t<T>* gmem) {
+  if constexpr (sizeof(C_t<T>) == 8) cp_async8(smem, gmem);
+  else cp_async16(smem, gmem);
+}
+
+// Factors of every line of one colour, for group blockIdx.y of the chunk:
+// the forward elimination of k_line_solve on records assembled in buf
+// (their right-hand sides unused), factors to fac (same record layout).
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m,
+                                                               const T* __restrict__ buf,
+                                                               T* __restrict__ fac) {
+  using V = typename Vec16<T>::V;
+  constexpr int NP = kPlanes<T>;
+  __shared__ V ring[kRing][NP][kSolveThreads];
+  const int grp = blockIdx.y;
+  const int tid = threadIdx.x;
+  const long l = blockIdx.x * (long)blockDim.x + tid;
+  if (l >= nl) return;
+  const V* base = reinterpret_cast<const V*>(buf) + (long)grp * m * NP * nl + l;
+  V* fout = reinterpret_cast<V*>(fac) + (long)grp * m * NP * nl + l;
+  const long rs = NP * nl;
+  auto issue = [&](int row) {
+    const V* src = base + (long)row * rs;
+    const int slot = row % kRing;
+#pragma unroll
+    for (int q = 0; q < NP; q++) cp_async16(&ring[slot][q][tid], src + q * nl);
+  };
+  C_t<T> W[21];
+#pragma unroll
+  for (int i = 0; i < 21; i++) W[i] = mk<T>(0, 0);
+#pragma unroll
+  for (int i = 0; i < 5; i++) W[WI(i, i)] = mk<T>(1, 0);
+  for (int p = 0; p < kRing - 1; p++) {
+    if (p < m) issue(p);
+    cp_async_commit();
+  }
+  for (int row = 0; row < m + 5; row++) {
+    if (row < m) {
+      if (row + kRing - 1 < m) issue(row + kRing - 1);
+      cp_async_commit();
+      cp_async_wait<kRing - 1>();
+      T nxt[kRec];
+      const int slot = row % kRing;
+#pragma unroll
+      for (int q = 0; q < NP; q++) unpack16(ring[slot][q][tid], nxt + q * kLanes<T>);
+#pragma unroll
+      for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(nxt[j], 0);
+      W[WI(5, 5)] = mk<T>(nxt[5], nxt[6]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
+      W[WI(5, 5)] = mk<T>(1, 0);
+    }
+    const C_t<T> id = crcp<T>(W[0]);
+    C_t<T> lq[6];
+#pragma unroll
+    for (int i = 1; i < 6; i++) lq[i] = cmul<T>(W[WI(i, 0)], id);
+#pragma unroll
+    for (int i = 1; i < 6; i++) {
+#pragma unroll
+      for (int j = 1; j <= i; j++) W[WI(i, j)] = cfms<T>(W[WI(i, j)], lq[i], W[WI(j, 0)]);
+    }
+    const int piv = row - 5;
+    if (piv >= 0) {
+      T o[kRec];
+#pragma unroll
+      for (int i = 1; i < 6; i++) {
+        o[2 * (i - 1)] = lq[i].x;
+        o[2 * (i - 1) + 1] = lq[i].y;
+      }
+      o[10] = id.x;
+      o[11] = id.y;
+      rec_put<T>(fout + (long)piv * rs, nl, o);
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+#pragma unroll
+      for (int j = 0; j <= i; j++) W[WI(i, j)] = W[WI(i + 1, j + 1)];
+    }
+  }
+  cp_async_wait<0>();
+}
+
+// Substitution with stored factors (group grp[rhs]): rb holds the rows'
+// residuals in, z between the passes, the correction x out.
+template <typename T>
+__global__ void __launch_bounds__(kSolveThreads) k_line_subst(const int* __restrict__ active,
+                                                              const int* __restrict__ grp,
+                                                              long nl, int m,
+                                                              const T* __restrict__ fac,
+                                                              C_t<T>* __restrict__ rb) {
+  using V = typename Vec16<T>::V;
+  constexpr int NP = kPlanes<T>;
+  __shared__ V ring[kRing][NP][kSolveThreads];
+  __shared__ C_t<T> rring[kRing][kSolveThreads];
+  const int rhs = blockIdx.y;
+  if (active && !active[rhs]) return;
+  const int tid = threadIdx.x;
+  const long l = blockIdx.x * (long)blockDim.x + tid;
+  if (l >= nl) return;
+  const long rs = NP * nl;
+  const V* fb = reinterpret_cast<const V*>(fac) + (long)grp[rhs] * m * rs + l;
+  C_t<T>* rr = rb + (long)rhs * m * nl + l;
+  auto issue_f = [&](int row) {
+    const V* src = fb + (long)row * rs;
+    const int slot = row % kRing;
+#pragma unroll
+    for (int q = 0; q < NP; q++) cp_async16(&ring[slot][q][tid], src + q * nl);
+  };
+  auto take_f = [&](int row, T (&v)[kRec]) {
+    const int slot = row % kRing;
+#pragma unroll
+    for (int q = 0; q < NP; q++) unpack16(ring[slot][q][tid], v + q * kLanes<T>);
+  };
+  // forward: at step `row` the residual of row `row` arrives and pivot
+  // row-5 is eliminated with its stored factors (k_line_solve's order)
+  C_t<T> y[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) y[i] = mk<T>(0, 0);
+  for (int p = 0; p < kRing - 1; p++) {
+    if (p < m) cp_async_c<T>(&rring[p % kRing][tid], rr + (long)p * nl);
+    if (p - 5 >= 0 && p - 5 < m) issue_f(p - 5);
+    cp_async_commit();
+  }
+  for (int row = 0; row < m + 5; row++) {
+    {
+      const int q = row + kRing - 1;
+      if (q < m) cp_async_c<T>(&rring[q % kRing][tid], rr + (long)q * nl);
+      if (q - 5 >= 0 && q - 5 < m) issue_f(q - 5);
+      cp_async_commit();
+    }
+    cp_async_wait<kRing - 1>();
+    y[5] = row < m ? rring[row % kRing][tid] : mk<T>(0, 0);
+    const int piv = row - 5;
+    if (piv >= 0) {
+      T v[kRec];
+      take_f(piv, v);
+#pragma unroll
+      for (int i = 1; i < 6; i++) y[i] = cfms<T>(y[i], mk<T>(v[2 * (i - 1)], v[2 * (i - 1) + 1]), y[0]);
+      rr[(long)piv * nl] = cmul<T>(y[0], mk<T>(v[10], v[11]));  // z
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) y[i] = y[i + 1];
+  }
+  cp_async_wait<0>();
+  __threadfence_block();  // z just stored is read back below
+  // backward: x_k = z_k - sum_i L(k+i, k) x_{k+i}
+  C_t<T> xw[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) xw[i] = mk<T>(0, 0);
+  for (int p = 0; p < kRing - 1; p++) {
+    const int q = m - 1 - p;
+    if (q >= 0) {
+      issue_f(q);
+      cp_async_c<T>(&rring[q % kRing][tid], rr + (long)q * nl);
+    }
+    cp_async_commit();
+  }
+  for (int row = m - 1; row >= 0; row--) {
+    {
+      const int q = row - (kRing - 1);
+      if (q >= 0) {
+        issue_f(q);
+        cp_async_c<T>(&rring[q % kRing][tid], rr + (long)q * nl);
+      }
+      cp_async_commit();
+    }
+    cp_async_wait<kRing - 1>();
+    T v[kRec];
+    take_f(row, v);
+    C_t<T> x = rring[row % kRing][tid];
+#pragma unroll
+    for (int i = 0; i < 5; i++) x = cfms<T>(x, mk<T>(v[2 * i], v[2 * i + 1]), xw[i]);
+#pragma unroll
+    for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
+    xw[0] = x;
+    rr[(long)row * nl] = x;
+  }
+  cp_async_wait<0>();
+}
+
+// u += x from rb[rhs][row][line]
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, int pb,
+                                                       const C_t<T>* __restrict__ rb) {
+  const int rhs = blockIdx.y;
+  if (L.active && !L.active[rhs]) return;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  long l;
+  int s;
+  if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
+  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  C_t<T>* u = L.u + (long)rhs * 3 * L.S;
+  const C_t<T>* x = rb + (long)rhs * g.m * g.nl + l;
+  const int r0 = 5 * (s - 1);
+  auto add = [&](long sl, int row) { u[sl] = cadd<T>(u[sl], x[(long)row * g.nl]); };
+  add(line_slot<D, 0>(L.n, L.S, ta, tb, s), r0);
+  if (s < g.nd) {
+    add(line_slot<D, 1>(L.n, L.S, ta, tb, s), r0 + 1);
+    add(line_slot<D, 2>(L.n, L.S, ta, tb, s), r0 + 2);
+    add(line_slot<D, 3>(L.n, L.S, ta, tb, s), r0 + 3);
+    add(line_slot<D, 4>(L.n, L.S, ta, tb, s), r0 + 4);
+  }
+}
+
+template <typename T, int D>
+static void line_factor_d(const LevelView<T>& L, int color, T* buf, T* fac, cudaStream_t st) {
+  const int pa = color & 1, pb = (color >> 1) & 1;
+  const long nl = line_count(L.n, D, color);
+  if (nl == 0) return;
+  const long items = nl * L.n[D];
+  const int m = 5 * L.n[D] - 4;
+  dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
+  k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
+  dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
+  k_line_factor<T><<<g2, kSolveThreads, 0, st>>>(nl, m, buf, fac);
+}
+
+template <typename T, int D>
+static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, const int* grp,
+                             C_t<T>* rb, cudaStream_t st) {
+  const int pa = color & 1, pb = (color >> 1) & 1;
+  const long nl = line_count(L.n, D, color);
+  if (nl == 0) return;
+  const long items = nl * L.n[D];
+  const int m = 5 * L.n[D] - 4;
+  dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
+  dim3 gr((unsigned)(((D == 0 ? 5 : 1) * items + 255) / 256), L.nrhs);
+  k_line_rhs<T, D><<<gr, 256, 0, st>>>(L, pa, pb, rb);
+  dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
+  k_line_subst<T><<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m, fac, rb);
+  k_line_apply_rb<T, D><<<g1, 256, 0, st>>>(L, pa, pb, rb);
+}
+
 template <typename T, int D>
 static void line_sweep_d(const LevelView<T>& L, int color, T* buf, cudaStream_t st) {
   const int pa = color & 1, pb = (color >> 1) & 1;
@@ -481,10 +869,31 @@ static void line_sweep_d(const LevelView<T>& L, int color, T* buf, cudaStream_t 
   const long items = nl * L.n[D];
   const int m = 5 * L.n[D] - 4;
   dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
-  k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
-  dim3 g2((unsigned)((nl + 63) / 64), L.nrhs);
-  k_line_solve<T><<<g2, 64, 0, st>>>(L.active, nl, m, buf);
+  if (D == 0) {
+    dim3 g5((unsigned)((5 * items + 255) / 256), L.nrhs);
+    k_line_assemble_rows<T, D><<<g5, 256, 0, st>>>(L, pa, pb, buf);
+  } else {
+    k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
+  }
+  dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
+  k_line_solve<T><<<g2, kSolveThreads, 0, st>>>(L.active, nl, m, buf);
   k_line_apply<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
+}
+
+// the line solve keeps a cp.async ring in shared memory: ask for the
+// largest shared-memory carveout so 12 blocks fit on an SM
+void init_line_kernels() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_line_solve<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_solve<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_subst<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_factor<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+  });
 }
 
 // scratch: m * lines * kRec values of T (see line_scratch_elems)
@@ -494,6 +903,27 @@ void launch_line_sweep(const LevelView<T>& L, int d, int color, C_t<T>* scratch,
   if (d == 0) line_sweep_d<T, 0>(L, color, buf, st);
   else if (d == 1) line_sweep_d<T, 1>(L, color, buf, st);
   else line_sweep_d<T, 2>(L, color, buf, st);
+}
+
+long line_factor_elems(const int n[3], int d, int color) {
+  return (long)(5 * n[d] - 4) * line_count(n, d, color) * kRec;
+}
+
+template <typename T>
+void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
+                        cudaStream_t st) {
+  T* buf = reinterpret_cast<T*>(scratch);
+  if (d == 0) line_factor_d<T, 0>(L, color, buf, fac, st);
+  else if (d == 1) line_factor_d<T, 1>(L, color, buf, fac, st);
+  else line_factor_d<T, 2>(L, color, buf, fac, st);
+}
+
+template <typename T>
+void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
+                           C_t<T>* rb, cudaStream_t st) {
+  if (d == 0) line_sweep_fac_d<T, 0>(L, color, fac, grp, rb, st);
+  else if (d == 1) line_sweep_fac_d<T, 1>(L, color, fac, grp, rb, st);
+  else line_sweep_fac_d<T, 2>(L, color, fac, grp, rb, st);
 }
 
 // ------------------------------------------------------------ point sweep
@@ -811,6 +1241,10 @@ void launch_zero(C_t<T>* p, long n, cudaStream_t st) {
   template void launch_zero<T>(C_t<T>*, long, cudaStream_t);
 EMMI_INST(float)
 EMMI_INST(double)
+template void launch_line_factor<float>(const LevelView<float>&, int, int, C_t<float>*, float*,
+                                        cudaStream_t);
+template void launch_line_sweep_fac<float>(const LevelView<float>&, int, int, const float*,
+                                           const int*, C_t<float>*, cudaStream_t);
 template void launch_residual<float, float>(const LevelView<float>&, C_t<float>*, double*, cudaStream_t);
 template void launch_residual<double, double>(const LevelView<double>&, C_t<double>*, double*, cudaStream_t);
 template void launch_residual<double, float>(const LevelView<double>&, C_t<float>*, double*, cudaStream_t);

@@ -4,11 +4,9 @@
 
 namespace emmi {
 
-// line-relaxation band table: for direction D, row type t (0: E_D(s-1),
-// 1: E_a(ta-1), 2: E_a(ta), 3: E_b(tb-1), 4: E_b(tb)) and neighbour k of the
-// row's edge equation, the band offset of that neighbour on the line, or
-// 127 if it is not a line unknown.  Filled once per process.
-void init_line_tables();
+// once per process, before any capture: kernel attributes of the line
+// relaxation (shared-memory carveout of the line solve)
+void init_line_kernels();
 
 template <typename T, typename TO>
 void launch_residual(const LevelView<T>& L, C_t<TO>* rout, double* norm2, cudaStream_t st);
@@ -24,6 +22,20 @@ template <typename T>
 void launch_line_sweep(const LevelView<T>& L, int d, int color, C_t<T>* scratch, cudaStream_t st);
 long line_count(const int n[3], int d, int color);
 long line_scratch_elems(const int n[3], int d, int nrhs);
+
+// stored LDL^T factors of the lines of one colour along d: T values per
+// operator group; launch_line_factor fills them for the L.nrhs groups of L
+// (L.op / L.wmu per group, u and f unused) through the record scratch into
+// fac + g * line_factor_elems; launch_line_sweep_fac then sweeps RHS r with
+// the factors of group grp[r], rb holding (5 n_d - 4) * lines complex values
+// per RHS
+long line_factor_elems(const int n[3], int d, int color);
+template <typename T>
+void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
+                        cudaStream_t st);
+template <typename T>
+void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
+                           C_t<T>* rb, cudaStream_t st);
 
 template <typename T>
 void launch_point_sweep(const LevelView<T>& L, int color, cudaStream_t st);

@@ -397,6 +397,7 @@ void emmi_default_options(emmi_options* o) {
   o->refine_every = 4;
   o->use_graphs = 1;
   o->verb = 0;
+  o->krylov = 0;
 }
 
 int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_options* opts) {
@@ -457,6 +458,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
       return EMMI_ECUDA;                                                         \
     }                                                                            \
   } while (0)
+  init_line_kernels();
   CKS(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
   CKS(cudaEventCreate(&s->ev0));
   CKS(cudaEventCreate(&s->ev1));
@@ -683,6 +685,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     while (s->chunk > 1 && (size_t)per_rhs * esz * s->chunk > cap) s->chunk = (s->chunk + 1) / 2;
     s->scratch_bytes = std::max<size_t>((size_t)per_rhs * esz * s->chunk, 16);
     TRY(s->alloc(&s->scratch, s->scratch_bytes));
+    if (mixed && s->opt.krylov > 0) TRY(krylov_alloc(s));
   }
 
   // ---- graphs
@@ -699,7 +702,9 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
 #undef CKS
 }
 
-static int run_part(emmi_solver* s, int h, int part) {
+}  // extern "C"
+
+int run_part(emmi_solver* s, int h, int part) {
   if (s->opt.use_graphs) {
     CK(cudaGraphLaunch(part ? s->gB[h] : s->gA[h], s->st));
     s->last_launches += part ? s->nodesB[h] : s->nodesA[h];
@@ -715,6 +720,8 @@ static int run_part(emmi_solver* s, int h, int part) {
   CK(cudaGetLastError());
   return EMMI_OK;
 }
+
+extern "C" {
 
 static int upload_mask(emmi_solver* s, int* dev, const std::vector<int>& host) {
   CK(cudaMemcpyAsync(dev, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice, s->st));
@@ -765,13 +772,17 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
   std::vector<double> nrm(nrhs), rnorm0(nrhs, 0.0), rn(nrhs, 0.0);
   std::vector<int> cycles(nrhs, 0), status(nrhs, EMMI_SOLVE_MAXIT), nref(nrhs, 0),
       since(nrhs, 0);
-  std::vector<double> best(nrhs, INFINITY);
+  std::vector<double> best(nrhs, INFINITY), last_rel(nrhs, 1.0);
   std::vector<int> stall(nrhs, 0);
+  s->h_fallback.assign(nrhs, 0);
+  s->h_learn.assign(nrhs, s->learned_on ? 1 : 0);
   if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
   const double tol = s->opt.tol;
   const int ncycle = s->opt.ncycle;
 
-  if (mixed) {
+  if (mixed && s->kry_m > 0) {
+    if ((rc = krylov_solve(s, cycles, status, nref, rnorm0, rn)) != EMMI_OK) return rc;
+  } else if (mixed) {
     // initial FP64 residual = b*vol (x = 0) -> f32[0]; rnorm0
     LevelView<double> V64 = s->view<double>(0, 0);
     V64.u = s->u64[0];
@@ -832,12 +843,18 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
             since[r] = 0;
             rn[r] = std::sqrt(nrm[r]);
             const double rel = rn[r] / rnorm0[r];
+            const double prev_rel = last_rel[r];
+            last_rel[r] = rel;
             if (!std::isfinite(rel)) {
               act[r] = 0;
               status[r] = EMMI_SOLVE_NONFINITE;
             } else if (rel <= tol) {
               act[r] = 0;
               status[r] = EMMI_SOLVE_OK;
+            } else if (rel > 0.5 * prev_rel && learned_fallback(s, r)) {
+              // no halving since the last refinement with the learned
+              // correction on: continue with plain cycles
+              stall[r] = 0;
             } else {
               if (rel < 0.5 * best[r]) {
                 best[r] = rel;
@@ -860,6 +877,8 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
         }
       }
       if ((rc = run_part(s, hh, 1)) != EMMI_OK) return rc;
+      if (s->learned_on && (rc = learned_after_cycle(s, hh, act)) != EMMI_OK) return rc;
+      if (s->ls_collect && (rc = learned_snapshot(s, hh, act)) != EMMI_OK) return rc;
       for (int r = 0; r < nrhs; r++)
         if (act[r]) {
           cycles[r]++;
@@ -975,6 +994,7 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
       stats[r].rnorm0 = rnorm0[r];
       stats[r].rnorm = rn[r];
       stats[r].refinements = nref[r];
+      stats[r].fallback = s->h_fallback[r];
     }
   return EMMI_OK;
 }

@@ -19,6 +19,7 @@ struct HLev {
 };
 
 void set_err(const char* fmt, ...);
+constexpr int kMaxKrylov = 12;
 }  // namespace emmi
 
 struct emmi_solver {
@@ -69,6 +70,39 @@ struct emmi_solver {
 
   std::vector<int> h_active, h_refine;
 
+  // FGMRES (MIXED, opt.krylov > 0): basis kv [m+1][nrhs][3S] FP64,
+  // preconditioned directions kz [m][nrhs][3S] complex64, FP64 temporaries
+  // kt (-z) and kw (A z) [nrhs][3S]; per RHS: Hessenberg column d_kh
+  // [nrhs][kMaxKrylov+1], solution weights d_ky [nrhs][kMaxKrylov], basis
+  // scale d_kscale and basis index d_kj
+  int kry_m = 0;
+  double2* kv = nullptr;
+  float2* kz = nullptr;
+  double2 *kt = nullptr, *kw = nullptr;
+  double2 *d_kh = nullptr, *d_ky = nullptr;
+  double* d_kscale = nullptr;
+  int* d_kj = nullptr;
+
+  // learned correction after each complex64 cycle (level 0): fp32 master and
+  // packed bf16 weights, bf16 input/hidden planes [nrhs][S][8], per-RHS
+  // enable mask (cleared for a RHS that falls back to plain cycles)
+  bool learned_on = false;
+  float* d_lsW = nullptr;
+  uint32_t* d_lsWp = nullptr;
+  uint32_t *d_lsX = nullptr, *d_lsH = nullptr;
+  int* d_learn = nullptr;
+  std::vector<int> h_learn, h_fallback;
+  // training set: complex64 level-0 residuals [cap][3][S], their |r|^2,
+  // operator and omega*mu0 per sample; snapshots are taken after each cycle
+  // of a solve while ls_collect is set, at most ls_per_rhs per RHS
+  bool ls_collect = false;
+  int ls_cap = 0, ls_count = 0, ls_per_rhs = 0;
+  float2* d_samples = nullptr;
+  double* d_srn2 = nullptr;
+  int* d_sop = nullptr;
+  float* d_swmu = nullptr;
+  std::vector<int> h_sop, h_taken;
+
   template <typename T> emmi::LevelView<T> view(int h, int l) const;
   template <typename T> void emit_smooth(int h, int l, int iter);
   template <typename T> void emit_cycle(int h, int l, int kind, int want, int& cur);
@@ -76,3 +110,23 @@ struct emmi_solver {
   template <typename T> int build_graphs();
   int alloc(void** p, size_t b);
 };
+
+// one part of a cycle on hierarchy h (graph launch or direct emission)
+int run_part(emmi_solver* s, int h, int part);
+
+namespace emmi {
+// FGMRES workspace for opt.krylov > 0 (called by emmi_solver_create)
+int krylov_alloc(emmi_solver* s);
+// FP64 FGMRES around complex64 cycles; expects f64[0] = b*vol and u64[0] = 0
+// on the solver's stream; fills the per-RHS statistics
+int krylov_solve(emmi_solver* s, std::vector<int>& cycles, std::vector<int>& status,
+                 std::vector<int>& nref, std::vector<double>& rnorm0, std::vector<double>& rn);
+// after a cycle on hierarchy h: the learned correction of the RHS that are
+// active and enabled (act = host copy of d_active)
+int learned_after_cycle(emmi_solver* s, int h, const std::vector<int>& act);
+// after a cycle: snapshot the level-0 complex64 residuals into the training set
+int learned_snapshot(emmi_solver* s, int h, const std::vector<int>& act);
+// a RHS that stalls with the learned correction drops back to plain cycles;
+// returns true when it did
+bool learned_fallback(emmi_solver* s, int r);
+}  // namespace emmi

@@ -50,12 +50,12 @@ class _Options(C.Structure):
     _fields_ = [("cycleopt", C.c_int), ("ncycle", C.c_int), ("v1", C.c_int), ("v2", C.c_int),
                 ("tol", C.c_double), ("isemicoarsen", C.c_int), ("precision", C.c_int),
                 ("sigma_floor", C.c_double), ("refine_every", C.c_int),
-                ("use_graphs", C.c_int), ("verb", C.c_int)]
+                ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int)]
 
 
 class _Stats(C.Structure):
     _fields_ = [("cycles", C.c_int), ("status", C.c_int), ("rnorm0", C.c_double),
-                ("rnorm", C.c_double), ("refinements", C.c_int)]
+                ("rnorm", C.c_double), ("refinements", C.c_int), ("fallback", C.c_int)]
 
 
 def lib():
@@ -103,11 +103,12 @@ class Options:
     refine_every: int = 4
     use_graphs: int = 1
     verb: int = 0
+    krylov: int = 0
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
                         self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
-                        self.verb)
+                        self.verb, self.krylov)
 
 
 class Solver:
@@ -198,7 +199,7 @@ class Solver:
     def _stats(st):
         return [dict(cycles=s.cycles, status=STATUS.get(s.status, s.status), rnorm0=s.rnorm0,
                      rnorm=s.rnorm, rel=(s.rnorm / s.rnorm0 if s.rnorm0 > 0 else 0.0),
-                     refinements=s.refinements) for s in st]
+                     refinements=s.refinements, fallback=s.fallback) for s in st]
 
     @property
     def stream(self) -> int:
@@ -213,6 +214,73 @@ class Solver:
                                                C.byref(nl), C.byref(by)),
                "emmi_solver_time_smoother")
         return ms.value, nl.value, by.value
+
+    # ---- learned correction after each complex64 cycle (MIXED solvers)
+    def learned_collect(self, b, per_rhs: int, device: bool = False):
+        """Residual samples of plain cycles: solve b ([nrhs, 3S] complex128
+        host array, or a device pointer with device=True) and keep the
+        level-0 residual after each of the first per_rhs cycles of every RHS.
+        Returns the solve statistics."""
+        st = (_Stats * self.nrhs)()
+        if device:
+            ptr = C.c_void_p(b)
+        else:
+            b = np.ascontiguousarray(b, np.complex128).reshape(self.nrhs, 3 * self.nslots)
+            ptr = _p(b)
+        _check(lib().emmi_learned_collect(self._h, ptr, 1 if device else 0, int(per_rhs), st),
+               "emmi_learned_collect")
+        return self._stats(st)
+
+    def inject_sources(self, src, chsrc=("Ex",)):
+        """Right-hand sides of unit dipoles src ([nrhs, 5] x, y, z, azimuth,
+        dip in radians) as a torch complex128 tensor [nrhs, 3S] on the GPU."""
+        import torch
+        srcd = torch.tensor(np.ascontiguousarray(src, np.float32).reshape(self.nrhs, 5),
+                            device="cuda")
+        ch = np.array([CHANNELS[c] for c in chsrc], np.int32)  # host: channel codes
+        b = torch.zeros((self.nrhs, 3 * self.nslots), dtype=torch.complex128, device="cuda")
+        torch.cuda.synchronize()
+        _check(lib().emmi_inject_sources_dev(self._h, C.c_void_p(srcd.data_ptr()), len(chsrc),
+                                             _p(ch), C.c_void_p(b.data_ptr())),
+               "emmi_inject_sources_dev")
+        torch.cuda.synchronize()
+        return b
+
+    def learned_add_samples(self, r, rhs):
+        """Add residual samples r ([ns, 3S] complex) of the operators of RHS
+        rhs[k] to the training set."""
+        r = np.ascontiguousarray(r, np.complex64).reshape(-1, 3 * self.nslots)
+        idx = np.ascontiguousarray(rhs, np.int32)
+        _check(lib().emmi_learned_add_samples(self._h, r.shape[0], _p(r), _p(idx)),
+               "emmi_learned_add_samples")
+
+    @property
+    def learned_samples(self) -> int:
+        return lib().emmi_learned_samples(self._h)
+
+    def learned_train(self, W, steps: int, lr: float = 1e-3):
+        """steps full-batch Adam steps on the GPU; returns (W, loss[steps])."""
+        W = np.ascontiguousarray(W, np.float32).copy()
+        loss = np.zeros(steps, np.float32)
+        _check(lib().emmi_learned_train(self._h, int(steps), C.c_float(lr), _p(W), _p(loss)),
+               "emmi_learned_train")
+        return W, loss
+
+    def learned_grad(self, W):
+        """(mean normalised loss, d(sum of normalised losses)/dW) at W."""
+        W = np.ascontiguousarray(W, np.float32)
+        loss = np.zeros(1, np.float32)
+        grad = np.zeros_like(W)
+        _check(lib().emmi_learned_grad(self._h, _p(W), _p(loss), _p(grad)), "emmi_learned_grad")
+        return float(loss[0]), grad
+
+    def set_learned(self, W):
+        """Apply W after every cycle of the following solves (None: off)."""
+        if W is None:
+            _check(lib().emmi_learned_set(self._h, None), "emmi_learned_set")
+            return
+        W = np.ascontiguousarray(W, np.float32)
+        _check(lib().emmi_learned_set(self._h, _p(W)), "emmi_learned_set")
 
     @property
     def last_time(self) -> float:

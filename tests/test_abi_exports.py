@@ -1,0 +1,55 @@
+"""Every function the C headers in include/ declare is exported by the
+library that implements it (no compute call: this runs without a GPU)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+PKG = os.path.join(ROOT, "libemmi_mgfd_gb300")
+LIBS = {"emmi_gpu.h": "libemmi_gpu.so", "emmi_dropin.h": "libemmi_gpu.so",
+        "emmi_host.h": "libemmi_host.so"}
+
+DECL = re.compile(r"^[A-Za-z_][\w \t\*]*?\b([A-Za-z_]\w*)\s*\(", re.M)
+
+
+def declared(header):
+    text = open(os.path.join(INCLUDE, header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"^\s*#.*$", "", text, flags=re.M)
+    names = []
+    for m in DECL.finditer(text):
+        line = text[m.start():text.find(";", m.start()) + 1]
+        if "typedef" in line or "(*" in line or not line.rstrip().endswith(";"):
+            continue
+        names.append(m.group(1))
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def built():
+    from libemmi_mgfd_gb300 import build as B
+    B.build()
+
+
+def test_headers_cover_the_libraries():
+    assert set(LIBS) == {f for f in os.listdir(INCLUDE) if f.endswith(".h")}
+
+
+@pytest.mark.parametrize("header", sorted(LIBS))
+def test_every_declared_function_is_exported(built, header):
+    names = declared(header)
+    assert names, header
+    lib = C.CDLL(os.path.join(PKG, LIBS[header]))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, (header, missing)
+
+
+def test_reference_entry_points_are_declared():
+    names = set(declared("emmi_dropin.h"))
+    for n in ("gmg_init", "gmg_apply", "gmg_free", "inject_source", "inject_adj_source",
+              "extract_emf_data", "extract_electric_field", "extract_magnetic_field",
+              "build_gradient"):
+        assert n in names, n

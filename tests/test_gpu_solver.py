@@ -91,16 +91,16 @@ def test_fp64_v_w_cycles_match_oracle(golden, cycleopt, ncyc):
 
 
 @gpu
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec,krylov", [(0, 0), (1, 0)])
 @pytest.mark.parametrize("name", ["tiny_layered", "tiny_aniso"])
-def test_converged_receivers_match_reference(golden, name, prec):
+def test_converged_receivers_match_reference(golden, name, prec, krylov):
     g = golden(name)
     # the fixture was solved by the reference to 1e-10; FP64 solves to the
-    # same.  Stationary complex64 refinement stalls near 7e-10 on tiny_aniso
-    # (air gradient modes converge at sigma_air/floor per refinement), so the
-    # mixed solve stops at 1e-9, still far inside the 1e-4 receiver bar.
+    # same.  On these 16^3 models with a large air layer the complex64
+    # preconditioner stops the mixed solver near 7e-10, so it solves to
+    # 1e-9, far inside the 1e-4 receiver bar.
     tol = 1e-10 if prec == 0 else 1e-9
-    s = _solver(g, precision=prec, ncycle=120, tol=tol)
+    s = _solver(g, precision=prec, ncycle=120, tol=tol, krylov=krylov)
     x, h, st = s.solve(g["b_f0"][None])
     assert st[0]["status"] == "ok", st
     assert st[0]["rel"] <= tol
