@@ -338,7 +338,8 @@ def main():
     traffic = ncu_traffic()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "kernel": "line sweep along x: k_line_assemble/k_line_solve/k_line_apply<float> (level 0, 4 colours, 25 RHS)",
+            "kernel": "level-0 line sweep along x, 4 colours x (k_line_rhs, k_line_subst, "
+                      "k_line_apply_rb)<float> with stored line factors, 25 RHS",
             "ms_per_sweep": round(ms, 4), "ms_per_sweep_xyz": ms_dir, "launches_per_sweep": nl,
             "algorithmic_bytes_per_launch": by / nl, "peak_kind": peak_kind}
     solver.close()

@@ -72,6 +72,10 @@ typedef struct {
   int krylov;       /* MIXED: 0 = stationary FP64 refinement of complex64
                        cycles; k > 0 = FP64 FGMRES(k) (k <= 12) with one
                        complex64 cycle as its preconditioner (0)           */
+  int line_factors; /* MIXED: 1 = factor every line once per (operator,
+                       frequency) at set-up and keep the factors, when they
+                       fit in half the free device memory; 0 = factor in
+                       every sweep (1)                                     */
 } emmi_options;
 
 typedef struct {

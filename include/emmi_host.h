@@ -63,6 +63,29 @@ int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *out);
 /* emf_init_free.c:114-128: the smallest resistivity of the three cubes */
 float eh_rho_water(const eh_model *m);
 
+/* ---- data misfit of the gradient mode (mode=2) ---------------------------
+ * Arrays of receiver data are [nchrec][nfreq][nrec], complex values as
+ * interleaved (re, im) floats; ch[] holds channel codes 0..5 = Ex, Ey, Ez,
+ * Hx, Hy, Hz. */
+
+/* cal_uncertainty_noise.c:17-97 without its noise: the standard deviation
+ * delta of every datum from the amplitude uncertainty amp_perc, the azimuth
+ * uncertainty delta_phi and the noise floors (Ez, Hz: 0, as the reference
+ * leaves them). */
+void eh_uncertainty(int nchrec, const int *ch, int nfreq, int nrec,
+                    const float *rec_azimuth, float src_azimuth,
+                    const float *dobs, float amp_perc, float delta_phi,
+                    float noisefloorE, float noisefloorH, float *delta);
+
+/* fg_fwi.c:208-226: for receivers farther than 5.5 skin depths of water from
+ * the source (horizontal offset), res = (dobs - dcal)/delta, rmse = |res|,
+ * the adjoint source dres = conj(res/delta); nearer receivers get dres = 0
+ * and rmse = 0.  Returns fcost = 0.5 * sum |res|^2. */
+float eh_misfit(int nchrec, int nfreq, int nrec, const float *omegas,
+                float rho_water, float src_x, float src_y, const float *rec_x,
+                const float *rec_y, const float *dobs, const float *dcal,
+                const float *delta, float *dres, float *rmse);
+
 #ifdef __cplusplus
 }
 #endif

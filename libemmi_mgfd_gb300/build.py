@@ -75,12 +75,14 @@ def build(force: bool = False, verbose: bool = False) -> None:
         _run([nvcc] + ARCH + ["-shared", "-o", GPU_LIB] + objs + ["-lcudart"])
     hsrc = [os.path.join(CSRC, f) for f in HOST_SOURCES if os.path.exists(os.path.join(CSRC, f))]
     if hsrc and (force or _stale(HOST_LIB, hsrc + headers)):
-        _run(["gcc", "-O2", "-fPIC", "-std=gnu99", "-shared", "-I" + INCLUDE, "-o", HOST_LIB]
+        _run(["gcc", "-O2", "-fPIC", "-std=gnu99", "-ffp-contract=off", "-shared", "-I" + INCLUDE,
+              "-o", HOST_LIB]
              + hsrc + ["-lm"])
     # the reference's modelling command line on the GPU path
     msrc = [os.path.join(CSRC, f) for f in MAIN_SOURCES]
     if force or _stale(MAIN_BIN, msrc + headers + [GPU_LIB]):
-        _run(["gcc", "-O2", "-std=gnu99", "-I" + INCLUDE, "-o", MAIN_BIN] + msrc
+        _run(["gcc", "-O2", "-std=gnu99", "-ffp-contract=off", "-I" + INCLUDE, "-o", MAIN_BIN]
+             + msrc
              + ["-L" + HERE, "-lemmi_gpu", "-Wl,-rpath,$ORIGIN", "-lm"])
 
 

@@ -11,6 +11,7 @@
  */
 #include "emmi_host.h"
 
+#include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -243,4 +244,94 @@ int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *g) {
   free(yy);
   free(zz);
   return rc;
+}
+
+/* ---- data misfit of the gradient mode --------------------------------- */
+/* The arithmetic keeps the reference's types: float data and uncertainty,
+ * double trigonometry and absolute values, float accumulation. */
+enum { EH_EX = 0, EH_EY = 1, EH_HX = 3, EH_HY = 4 };
+
+static float complex datum(const float *a, long i) { return a[2 * i] + I * a[2 * i + 1]; }
+
+void eh_uncertainty(int nchrec, const int *ch, int nfreq, int nrec, const float *rec_azimuth,
+                    float src_azimuth, const float *dobs, float amp_perc, float delta_phi,
+                    float noisefloorE, float noisefloorH, float *delta) {
+  memset(delta, 0, (size_t)nchrec * nfreq * nrec * sizeof(float));
+  for (int ir = 0; ir < nrec; ir++) {
+    const float phi = rec_azimuth[ir] - src_azimuth;  /* receiver vs towline */
+    for (int f = 0; f < nfreq; f++) {
+      /* the horizontal components and their rotation into the towline */
+      float complex ex = 0, ey = 0, hx = 0, hy = 0, exc = 0, eyc = 0, hxc = 0, hyc = 0;
+      for (int c = 0; c < nchrec; c++) {
+        const float complex v = datum(dobs, ((long)c * nfreq + f) * nrec + ir);
+        switch (ch[c]) {
+          case EH_EX: ex = v; exc += ex * cos(phi); eyc += ex * sin(phi); break;
+          case EH_EY: ey = v; exc -= ey * sin(phi); eyc += ey * cos(phi); break;
+          case EH_HX: hx = v; hxc += hx * cos(phi); hyc += hx * sin(phi); break;
+          case EH_HY: hy = v; hxc -= hy * sin(phi); hyc += hy * cos(phi); break;
+          default: break;
+        }
+      }
+      for (int c = 0; c < nchrec; c++) {
+        float s1, s2, s3, nf;
+        switch (ch[c]) {
+          case EH_EX:
+            s1 = cabs(amp_perc * ex) * cos(phi);
+            s2 = cabs(amp_perc * ey) * sin(phi);
+            s3 = delta_phi * cabs(eyc);
+            nf = noisefloorE;
+            break;
+          case EH_EY:
+            s1 = cabs(amp_perc * ex) * sin(phi);
+            s2 = cabs(amp_perc * ey) * cos(phi);
+            s3 = delta_phi * cabs(exc);
+            nf = noisefloorE;
+            break;
+          case EH_HX:
+            s1 = cabs(amp_perc * hx) * cos(phi);
+            s2 = cabs(amp_perc * hy) * sin(phi);
+            s3 = delta_phi * cabs(hyc);
+            nf = noisefloorH;
+            break;
+          case EH_HY:  /* the reference scales inside the modulus here */
+            s1 = cabs(amp_perc * hx) * sin(phi);
+            s2 = cabs(amp_perc * hy) * cos(phi);
+            s3 = cabs(delta_phi * hxc);
+            nf = noisefloorH;
+            break;
+          default:
+            continue;
+        }
+        delta[((long)c * nfreq + f) * nrec + ir] = sqrt(s1 * s1 + s2 * s2 + s3 * s3 + nf * nf);
+      }
+    }
+  }
+}
+
+float eh_misfit(int nchrec, int nfreq, int nrec, const float *omegas, float rho_water, float src_x,
+                float src_y, const float *rec_x, const float *rec_y, const float *dobs,
+                const float *dcal, const float *delta, float *dres, float *rmse) {
+  const double mu0 = 4. * 3.14159265358979323846264 * 1e-7;
+  memset(dres, 0, (size_t)nchrec * nfreq * nrec * 2 * sizeof(float));
+  memset(rmse, 0, (size_t)nchrec * nfreq * nrec * sizeof(float));
+  float fcost = 0.f;
+  for (int c = 0; c < nchrec; c++)
+    for (int f = 0; f < nfreq; f++) {
+      const float skin = 5.5 * sqrt(2. * rho_water / (omegas[f] * mu0));
+      for (int ir = 0; ir < nrec; ir++) {
+        const float ox = rec_x[ir] - src_x, oy = rec_y[ir] - src_y;
+        if (!(sqrt(ox * ox + oy * oy) > skin)) continue;
+        const long i = ((long)c * nfreq + f) * nrec + ir;
+        float complex r = datum(dobs, i) - datum(dcal, i);
+        r /= delta[i];
+        rmse[i] = cabs(r);
+        fcost += r * conj(r);
+        r /= delta[i];
+        r = conj(r);
+        dres[2 * i] = crealf(r);
+        dres[2 * i + 1] = cimagf(r);
+      }
+    }
+  fcost *= 0.5;
+  return fcost;
 }

@@ -138,8 +138,12 @@ __global__ void __launch_bounds__(256) k_ls_input(LevelView<float> L, const floa
 }
 
 // ---------------------------------------------------------------- conv
-// One 3x3x3 convolution, 8 -> 8 channels, on the tensor cores.  A warp owns
-// 16 consecutive slots of one (j, k) row per tile.
+// One 3x3x3 convolution, 8 -> 8 channels, on the tensor cores.  A block of
+// 4 warps owns a brick of 48 x 2 x 2 slots (i, j, k): it stages the brick
+// and its one-slot halo (50 x 4 x 4 slots x 16 bytes) in shared memory with
+// coalesced loads, then each warp computes 3 of the brick's 12 m-tiles
+// (16 consecutive slots along i) with A fragments read from shared memory
+// (8 consecutive slots x 4 words per load: conflict-free).
 //   MODE 0: out = hidden layer, bf16 [b][S][8]
 //   MODE 1: u += channels 0..5 on unknown edges (deployment)
 //   MODE 2: c = channels 0..5 on unknown edges, 0 elsewhere ([b][3][S])
@@ -147,18 +151,36 @@ struct ConvArgs {
   int n[3];      // cells of the level
   int X, Y, Z;   // slots per direction (n+1)
   long S;
-  int tiles;     // m-tiles per RHS
+  int tiles;     // bricks per RHS
   const int* mask;
 };
+
+constexpr int kBI = 48, kBJ = 2, kBK = 2;
+constexpr int kHI = kBI + 2, kHJ = kBJ + 2, kHK = kBK + 2;
 
 template <int MODE>
 __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint32_t* __restrict__ in,
                                                  const uint32_t* __restrict__ Wp,
                                                  uint32_t* __restrict__ hid,
                                                  float2* __restrict__ out) {
+  __shared__ uint4 halo[kHK * kHJ * kHI];
   const int b = blockIdx.y;
   if (a.mask && !a.mask[b]) return;
-  const int lane = threadIdx.x & 31;
+  const int nbi = (a.X + kBI - 1) / kBI, nbj = (a.Y + kBJ - 1) / kBJ;
+  const int brick = blockIdx.x;
+  const int bi0 = (brick % nbi) * kBI;
+  const int bj0 = ((brick / nbi) % nbj) * kBJ;
+  const int bk0 = (brick / (nbi * nbj)) * kBK;
+  const uint4* inb = reinterpret_cast<const uint4*>(in) + (long)b * a.S;
+  for (int q = threadIdx.x; q < kHK * kHJ * kHI; q += blockDim.x) {
+    const int hi = q % kHI, hj = (q / kHI) % kHJ, hk = q / (kHI * kHJ);
+    const int i = bi0 + hi - 1, j = bj0 + hj - 1, k = bk0 + hk - 1;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (i >= 0 && i < a.X && j >= 0 && j < a.Y && k >= 0 && k < a.Z)
+      v = inb[((long)k * a.Y + j) * a.X + i];
+    halo[q] = v;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, t4 = lane & 3;
   uint32_t bw[kKSteps][2];
 #pragma unroll
@@ -166,30 +188,29 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint32_t* __r
     bw[ks][0] = Wp[(ks * 32 + lane) * 2];
     bw[ks][1] = Wp[(ks * 32 + lane) * 2 + 1];
   }
-  const uint32_t* inb = in + (long)b * a.S * 4;
-  const int mt = (a.X + 15) >> 4;
-  const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < a.tiles;
-       tile += warps) {
-    const int row = tile / mt;
-    const int i0 = (tile - row * mt) * 16;
-    const int j = row % a.Y, k = row / a.Y;
-    const int iA = i0 + g, iB = i0 + g + 8;
-    auto ld = [&](int i, int di, int dj, int dk) -> uint32_t {
-      const int ii = i + di, jj = j + dj, kk = k + dk;
-      if (i >= a.X || ii < 0 || ii >= a.X || jj < 0 || jj >= a.Y || kk < 0 || kk >= a.Z) return 0u;
-      return inb[(((long)kk * a.Y + jj) * a.X + ii) * 4 + t4];
+  __syncthreads();
+  const uint32_t* hw = reinterpret_cast<const uint32_t*>(halo);
+  for (int tl = warp; tl < (kBI / 16) * kBJ * kBK; tl += blockDim.x >> 5) {
+    const int ib = tl % (kBI / 16), jl = (tl / (kBI / 16)) % kBJ, kl = tl / ((kBI / 16) * kBJ);
+    const int j = bj0 + jl, k = bk0 + kl;
+    if (j >= a.Y || k >= a.Z) continue;  // warp-uniform
+    const int iA = bi0 + 16 * ib + g, iB = iA + 8;
+    // halo word of the slot at local i offset li, shifted by tap t
+    auto ld = [&](int li, int t) -> uint32_t {
+      const int hi = li + 1 + tap_di(t), hj = jl + 1 + tap_dj(t), hk = kl + 1 + tap_dk(t);
+      return hw[((hk * kHJ + hj) * kHI + hi) * 4 + t4];
     };
+    const int liA = 16 * ib + g, liB = liA + 8;
     float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
 #pragma unroll
     for (int ks = 0; ks < kKSteps; ks++) {
       const int t0 = 2 * ks, t1 = 2 * ks + 1;
-      const uint32_t a0 = ld(iA, tap_di(t0), tap_dj(t0), tap_dk(t0));
-      const uint32_t a1 = ld(iB, tap_di(t0), tap_dj(t0), tap_dk(t0));
+      const uint32_t a0 = ld(liA, t0);
+      const uint32_t a1 = ld(liB, t0);
       uint32_t a2 = 0u, a3 = 0u;
       if (t1 < kTaps) {
-        a2 = ld(iA, tap_di(t1), tap_dj(t1), tap_dk(t1));
-        a3 = ld(iB, tap_di(t1), tap_dj(t1), tap_dk(t1));
+        a2 = ld(liA, t1);
+        a3 = ld(liB, t1);
       }
       asm volatile(
           "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
@@ -360,17 +381,13 @@ ConvArgs conv_args(const int n[3], int nb, const int* mask) {
   a.Y = n[1] + 1;
   a.Z = n[2] + 1;
   a.S = (long)a.X * a.Y * a.Z;
-  a.tiles = ((a.X + 15) / 16) * a.Y * a.Z;
+  a.tiles = ((a.X + kBI - 1) / kBI) * ((a.Y + kBJ - 1) / kBJ) * ((a.Z + kBK - 1) / kBK);
   a.mask = mask;
   (void)nb;
   return a;
 }
 
-unsigned conv_blocks(const ConvArgs& a) {
-  // 4 warps per block, one tile per warp per pass; up to 8 blocks per SM
-  const long need = (a.tiles + 3) / 4;
-  return (unsigned)std::max(1L, std::min(need, 152L * 8));
-}
+unsigned conv_blocks(const ConvArgs& a) { return (unsigned)a.tiles; }
 
 }  // namespace
 

@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "emmi_gpu.h"
@@ -126,6 +127,34 @@ __global__ void k_scale_dual(const double2* __restrict__ b, double2* __restrict_
   for (int c = 0; c < 3; c++) {
     const double2 v = b[base + c * S + s];
     f[base + c * S + s] = make_double2(v.x * w[c], v.y * w[c]);
+  }
+}
+
+// The first residual of a mixed solve, where x = 0: r = b*vol exactly, so
+// f32 = (float) f64, u32 = 0 and |r|^2 need no operator application
+__global__ void __launch_bounds__(256) k_first_residual(const double2* __restrict__ f64,
+                                                        float2* __restrict__ f32,
+                                                        float2* __restrict__ u32, long n3s,
+                                                        const int* __restrict__ mask,
+                                                        double* __restrict__ norm2) {
+  const int rhs = blockIdx.y;
+  if (mask && !mask[rhs]) return;
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n3s; i += (long)gridDim.x * blockDim.x) {
+    const double2 v = f64[(long)rhs * n3s + i];
+    f32[(long)rhs * n3s + i] = make_float2((float)v.x, (float)v.y);
+    u32[(long)rhs * n3s + i] = make_float2(0.f, 0.f);
+    acc += v.x * v.x + v.y * v.y;
+  }
+  __shared__ double red[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) v += red[k];
+    atomicAdd(norm2 + rhs, v);
   }
 }
 
@@ -249,6 +278,25 @@ LevelView<float> emmi_solver::view<float>(int h, int l) const {
   return V;
 }
 
+// one colour of line relaxation along d on level l of hierarchy h for the
+// RHS chunk W starting at r0: with the stored factors of the colour when the
+// complex64 solver keeps them, else factoring in the sweep
+template <typename T>
+static void line_colour(emmi_solver* s, int h, int l, int d, int col, const LevelView<T>& W,
+                        int r0) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (s->fac_on) {
+      const long off = s->fac_off[l == 0 ? 0 : h][l][d][col];
+      if (off >= 0) {
+        launch_line_sweep_fac<float>(W, d, col, s->d_fac + off, s->d_grp + r0,
+                                     (C_t<float>*)s->scratch, s->st);
+        return;
+      }
+    }
+  }
+  launch_line_sweep<T>(W, d, col, (C_t<T>*)s->scratch, s->st);
+}
+
 // smoothing (gmg.c:1301-1313): line relaxation along every direction the
 // next level coarsens, else node-patch relaxation; odd iter reverses colours
 template <typename T>
@@ -270,8 +318,8 @@ void emmi_solver::emit_smooth(int h, int l, int iter) {
           W.wmu += r0;
           W.active += r0;
           W.op += r0;
-          launch_line_sweep<T>(W, d, col, (C_t<T>*)scratch, st);
-          launch_counter += 3;  // assemble, solve, apply
+          line_colour<T>(this, h, l, d, col, W, r0);
+          launch_counter += 3;  // assemble (residual), solve, apply
         }
       }
     }
@@ -380,6 +428,96 @@ int emmi_solver::build_graphs() {
   return EMMI_OK;
 }
 
+// Stored line factors of the complex64 cycle: group the RHS by (operator,
+// frequency), size the factor blocks of every (hierarchy, level, direction,
+// colour) the smoother relaxes, and factor each group's lines once.  Leaves
+// fac_on false (factoring in every sweep) when they would take more than
+// half of the free device memory.
+static int build_line_factors(emmi_solver* s) {
+  const int nrhs = s->nrhs;
+  std::vector<int> grp(nrhs), gop;
+  std::vector<float> gw;
+  for (int r = 0; r < nrhs; r++) {
+    const float w = (float)((double)s->h_omega[r] * kMu0);
+    int g = -1;
+    for (int k = 0; k < (int)gop.size() && g < 0; k++)
+      if (gop[k] == s->h_op[r] && gw[k] == w) g = k;
+    if (g < 0) {
+      g = (int)gop.size();
+      gop.push_back(s->h_op[r]);
+      gw.push_back(w);
+    }
+    grp[r] = g;
+  }
+  const int ng = (int)gop.size();
+  for (int h = 0; h < 3; h++)
+    for (int l = 0; l < emmi::kMaxLev; l++)
+      for (int d = 0; d < 3; d++)
+        for (int c = 0; c < 4; c++) s->fac_off[h][l][d][c] = -1;
+  // level 0 is the same in every hierarchy: its blocks live under h = 0
+  long total = 0;
+  for (int h = 0; h < 3; h++)
+    for (int l = 0; l + 1 < s->lmax; l++)
+      for (int d = 0; d < 3; d++) {
+        if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
+        const int hb = l == 0 ? 0 : h;
+        if (s->fac_off[hb][l][d][0] >= 0) continue;
+        for (int c = 0; c < 4; c++) {
+          s->fac_off[hb][l][d][c] = total;
+          total += (long)ng * line_factor_elems(s->hier[h][l].n, d, c);
+        }
+      }
+  if (total == 0) return EMMI_OK;
+  size_t freeb = 0, totb = 0;
+  CK(cudaMemGetInfo(&freeb, &totb));
+  const size_t bytes = (size_t)total * sizeof(float);
+  if (bytes > freeb / 2) return EMMI_OK;  // factor in every sweep instead
+  int rc;
+  if ((rc = s->alloc((void**)&s->d_fac, bytes)) != EMMI_OK) return rc;
+  if ((rc = s->alloc((void**)&s->d_grp, nrhs * sizeof(int))) != EMMI_OK) return rc;
+  if ((rc = s->alloc((void**)&s->d_gop, ng * sizeof(int))) != EMMI_OK) return rc;
+  if ((rc = s->alloc((void**)&s->d_gwmu, ng * sizeof(float))) != EMMI_OK) return rc;
+  CK(cudaMemcpyAsync(s->d_grp, grp.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->d_gop, gop.data(), ng * sizeof(int), cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->d_gwmu, gw.data(), ng * sizeof(float), cudaMemcpyHostToDevice, s->st));
+  s->ngroups = ng;
+  s->fac_bytes = bytes;
+  // factor every block once: records assembled into the scratch for `chunk`
+  // groups at a time (u and f of the level are read but their residual is
+  // not used)
+  std::vector<long> done;
+  for (int h = 0; h < 3; h++)
+    for (int l = 0; l + 1 < s->lmax; l++)
+      for (int d = 0; d < 3; d++) {
+        if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
+        const int hb = l == 0 ? 0 : h;
+        const long off0 = s->fac_off[hb][l][d][0];
+        if (std::find(done.begin(), done.end(), off0) != done.end()) continue;
+        done.push_back(off0);
+        LevelView<float> V = s->view<float>(h, l);
+        V.op = s->d_gop;
+        V.wmu = s->d_gwmu;
+        V.active = nullptr;
+        for (int c = 0; c < 4; c++) {
+          const long per = line_factor_elems(s->hier[h][l].n, d, c);
+          for (int g0 = 0; g0 < ng; g0 += s->chunk) {
+            LevelView<float> W = V;
+            W.nrhs = std::min(s->chunk, ng - g0);
+            W.u += (long)g0 * 3 * V.S;
+            W.f += (long)g0 * 3 * V.S;
+            W.op += g0;
+            W.wmu += g0;
+            launch_line_factor<float>(W, d, c, (C_t<float>*)s->scratch,
+                                      s->d_fac + s->fac_off[hb][l][d][c] + (long)g0 * per, s->st);
+          }
+        }
+      }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s->st));
+  s->fac_on = true;
+  return EMMI_OK;
+}
+
 // ============================================================ C ABI
 extern "C" {
 
@@ -398,6 +536,7 @@ void emmi_default_options(emmi_options* o) {
   o->use_graphs = 1;
   o->verb = 0;
   o->krylov = 0;
+  o->line_factors = 1;
 }
 
 int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_options* opts) {
@@ -686,6 +825,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     s->scratch_bytes = std::max<size_t>((size_t)per_rhs * esz * s->chunk, 16);
     TRY(s->alloc(&s->scratch, s->scratch_bytes));
     if (mixed && s->opt.krylov > 0) TRY(krylov_alloc(s));
+    if (mixed && s->opt.line_factors) TRY(build_line_factors(s));
   }
 
   // ---- graphs
@@ -783,16 +923,14 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
   if (mixed && s->kry_m > 0) {
     if ((rc = krylov_solve(s, cycles, status, nref, rnorm0, rn)) != EMMI_OK) return rc;
   } else if (mixed) {
-    // initial FP64 residual = b*vol (x = 0) -> f32[0]; rnorm0
-    LevelView<double> V64 = s->view<double>(0, 0);
-    V64.u = s->u64[0];
-    V64.f = s->f64[0];
-    V64.active = s->d_active;
+    // initial FP64 residual = b*vol (x = 0) -> f32[0]; rnorm0; u32 = 0
     CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
-    launch_residual<double, float>(V64, s->f32[0], s->d_norm64, s->st);
-    s->last_launches++;
-    launch_zero<float>(s->u32[0], n3s * nrhs, s->st);
-    s->last_launches++;
+    {
+      dim3 g(blocks_for(n3s, 256, 2048), nrhs);
+      k_first_residual<<<g, 256, 0, s->st>>>(s->f64[0], s->f32[0], s->u32[0], n3s, s->d_active,
+                                             s->d_norm64);
+      s->last_launches++;
+    }
     if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
     for (int r = 0; r < nrhs; r++) {
       rnorm0[r] = std::sqrt(nrm[r]);
@@ -1042,7 +1180,7 @@ int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int
           W.wmu += r0;
           W.active += r0;
           W.op += r0;
-          launch_line_sweep<float>(W, dir, cc, (C_t<float>*)s->scratch, s->st);
+          line_colour<float>(s, h, 0, dir, cc, W, r0);
         } else {
           LevelView<double> W = s->view<double>(h, 0);
           W.nrhs = nr;
@@ -1052,7 +1190,7 @@ int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int
           W.wmu += r0;
           W.active += r0;
           W.op += r0;
-          launch_line_sweep<double>(W, dir, cc, (C_t<double>*)s->scratch, s->st);
+          line_colour<double>(s, h, 0, dir, cc, W, r0);
         }
       }
   };

@@ -70,6 +70,19 @@ struct emmi_solver {
 
   std::vector<int> h_active, h_refine;
 
+  // stored line factors (MIXED, opt.line_factors): RHS sharing an operator
+  // and a frequency form a group; d_fac holds the LDL^T factors of every
+  // line per group, in blocks per (hierarchy, level, direction, colour) at
+  // float offsets fac_off (-1: none; level 0 is shared by the hierarchies)
+  bool fac_on = false;
+  int ngroups = 0;
+  int* d_grp = nullptr;     // [nrhs] group of each RHS
+  int* d_gop = nullptr;     // [ngroups] operator of each group
+  float* d_gwmu = nullptr;  // [ngroups] omega*mu0 of each group
+  float* d_fac = nullptr;
+  size_t fac_bytes = 0;
+  long fac_off[3][emmi::kMaxLev][3][4];
+
   // FGMRES (MIXED, opt.krylov > 0): basis kv [m+1][nrhs][3S] FP64,
   // preconditioned directions kz [m][nrhs][3S] complex64, FP64 temporaries
   // kt (-z) and kw (A z) [nrhs][3S]; per RHS: Hessenberg column d_kh

@@ -50,7 +50,8 @@ class _Options(C.Structure):
     _fields_ = [("cycleopt", C.c_int), ("ncycle", C.c_int), ("v1", C.c_int), ("v2", C.c_int),
                 ("tol", C.c_double), ("isemicoarsen", C.c_int), ("precision", C.c_int),
                 ("sigma_floor", C.c_double), ("refine_every", C.c_int),
-                ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int)]
+                ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int),
+                ("line_factors", C.c_int)]
 
 
 class _Stats(C.Structure):
@@ -104,11 +105,12 @@ class Options:
     use_graphs: int = 1
     verb: int = 0
     krylov: int = 0
+    line_factors: int = 1
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
                         self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
-                        self.verb, self.krylov)
+                        self.verb, self.krylov, self.line_factors)
 
 
 class Solver:

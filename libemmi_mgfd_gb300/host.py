@@ -1,5 +1,6 @@
 """ctypes front of libemmi_host.so: the C host front end (regridding and
-homogenization) that prepares each shot's mesh and conductivities."""
+homogenization) that prepares each shot's mesh and conductivities, and the
+data misfit of the gradient mode."""
 from __future__ import annotations
 
 import ctypes as C
@@ -21,7 +22,54 @@ def lib():
         _lib = C.CDLL(HOST_LIB)
         _lib.eh_create_nugrid.restype = C.c_float
         _lib.eh_rho_water.restype = C.c_float
+        _lib.eh_misfit.restype = C.c_float
+        _lib.eh_misfit.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_float,
+                                   C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.eh_uncertainty.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                        C.c_float, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                                        C.c_float, C.c_void_p]
     return _lib
+
+
+CHANNELS = {"Ex": 0, "Ey": 1, "Ez": 2, "Hx": 3, "Hy": 4, "Hz": 5}
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def uncertainty(chrec, dobs, rec_azimuth, src_azimuth, amp_perc=0.03, delta_phi=0.0,
+                noisefloorE=1e-15, noisefloorH=1e-13):
+    """Standard deviation of every datum (cal_uncertainty_noise.c:17-97,
+    without the noise): dobs complex64 [nchrec, nfreq, nrec]."""
+    dobs = np.ascontiguousarray(dobs, np.complex64)
+    nch, nf, nr = dobs.shape
+    ch = np.array([CHANNELS[c] for c in chrec], np.int32)
+    az = np.ascontiguousarray(rec_azimuth, np.float32)
+    delta = np.zeros(dobs.shape, np.float32)
+    lib().eh_uncertainty(nch, _ptr(ch), nf, nr, _ptr(az), C.c_float(src_azimuth), _ptr(dobs),
+                         C.c_float(amp_perc), C.c_float(delta_phi), C.c_float(noisefloorE),
+                         C.c_float(noisefloorH), _ptr(delta))
+    return delta
+
+
+def misfit(dobs, dcal, delta, omegas, rho_water, src_xy, rec_x, rec_y):
+    """fg_fwi.c:208-226: (fcost, dres, rmse) for one shot; arrays
+    [nchrec, nfreq, nrec]."""
+    dobs = np.ascontiguousarray(dobs, np.complex64)
+    dcal = np.ascontiguousarray(dcal, np.complex64)
+    delta = np.ascontiguousarray(delta, np.float32)
+    nch, nf, nr = dobs.shape
+    om = np.ascontiguousarray(omegas, np.float32)
+    rx = np.ascontiguousarray(rec_x, np.float32)
+    ry = np.ascontiguousarray(rec_y, np.float32)
+    dres = np.zeros_like(dobs)
+    rmse = np.zeros(dobs.shape, np.float32)
+    f = lib().eh_misfit(nch, nf, nr, _ptr(om), C.c_float(rho_water), C.c_float(src_xy[0]),
+                        C.c_float(src_xy[1]), _ptr(rx), _ptr(ry), _ptr(dobs), _ptr(dcal),
+                        _ptr(delta), _ptr(dres), _ptr(rmse))
+    return float(f), dres, rmse
 
 
 class _Model(C.Structure):

@@ -7,7 +7,8 @@ slot fields, receiver data, volume extractions, adjoint sources and the
 mode=2 gradient -- as compressed .npz files.  The reference does not exist on
 GPU machines; these fixtures carry its outputs there.
 
-    python tests/golden/make_golden.py          (needs oracle/_ref built)
+    python tests/golden/make_golden.py            (needs oracle/_ref built)
+    python tests/golden/make_golden.py tiny_grad  (the mode=2 gradient case only)
 """
 from __future__ import annotations
 
@@ -24,6 +25,7 @@ sys.path.insert(0, ROOT)
 from libemmi_mgfd_gb300 import workloads as W  # noqa: E402
 
 REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+REF_MAIN = os.path.join(ROOT, "oracle", "_ref", "emmi_ref")
 
 
 def run_ref(s: W.Survey, extra, adjoint: int):
@@ -91,9 +93,63 @@ def case(s: W.Survey, extra, adjoint=0, keep_fields=True, nfreq=1, tag=None):
     return rec
 
 
+def start_model(s: W.Survey) -> W.Survey:
+    """The starting model of the gradient case: the resistive layer of the
+    layered model removed (1 ohm-m below the water)."""
+    rho = np.where(s.rho11 > 10.0, 1.0, s.rho11).astype(np.float32)
+    return W.Survey(s.name + "_start", s.nx, s.ny, s.nz, s.dx, s.dy, s.dz, s.ox, s.oy, s.oz,
+                    rho, rho.copy(), rho.copy(), s.sources, s.receivers, s.pairs, s.freqs, s.n,
+                    s.chsrc, s.chrec, dict(s.extra), s.bathy)
+
+
+def mode2_case(tol="1e-10"):
+    """The reference's main in mode=2 (one data gradient, src/fg_fwi.c):
+    observed data from a mode=0 run on the layered model, gradient of the
+    start model, without noise."""
+    true = W.tiny_layered()
+    start = start_model(true)
+    d = tempfile.mkdtemp(prefix="golden_m2_")
+    true.write(os.path.join(d, "true"))
+    start.write(d)
+    common = [f"tol={tol}", "ncycle=80"]
+    r0 = subprocess.run([REF_MAIN] + true.params(os.path.join(d, "true")) + common, cwd=d,
+                        capture_output=True, text=True)
+    if r0.returncode != 0:
+        raise RuntimeError(r0.stdout + r0.stderr)
+    obs_text = open(os.path.join(d, "emf_0001.txt")).read()
+    args = [a for a in start.params(d) if not a.startswith("mode=") and not a.startswith("verb=")]
+    args += ["mode=2", "verb=1", "addnoise=0", "npar=2", "idxpar=1,2", "preco=1"] + common
+    r2 = subprocess.run([REF_MAIN] + args, cwd=d, capture_output=True, text=True)
+    if r2.returncode != 0:
+        raise RuntimeError(r2.stdout + r2.stderr)
+    n = start.nx * start.ny * start.nz
+    fcost = [float(l.split("fcost=")[1].split(",")[0]) for l in r2.stdout.splitlines()
+             if l.startswith("isrc=")]
+    rm = np.loadtxt(os.path.join(d, "rmse_0001.txt"), skiprows=1, usecols=(4,))
+    syn = np.loadtxt(os.path.join(d, "syn_0001.txt"), skiprows=1, usecols=(4, 5))
+    return {
+        "name": np.array("tiny_grad"),
+        "params": np.array(" ".join(args[-6:])),
+        "rho_true": true.rho11, "rho_start": start.rho11,
+        "obs_text": np.array(obs_text),
+        "grad_Rv": np.fromfile(os.path.join(d, "gradient_dat_Rv"), np.float32, n),
+        "grad_Rh": np.fromfile(os.path.join(d, "gradient_dat_Rh"), np.float32, n),
+        "rmse": rm.astype(np.float32),
+        "syn": (syn[:, 0] + 1j * syn[:, 1]).astype(np.complex64),
+        "fcost": np.array(fcost, np.float64),
+        "stdout": np.array(r2.stdout[-4000:]),
+    }
+
+
 def main():
     if not os.path.exists(REF_DUMP):
         sys.exit("oracle/_ref/ref_dump missing: run `make -C oracle ref` first")
+    only = set(sys.argv[1:])
+    if only == {"tiny_grad"}:
+        rec = mode2_case()
+        np.savez_compressed(os.path.join(HERE, "tiny_grad.npz"), **rec)
+        print("tiny_grad", os.path.getsize(os.path.join(HERE, "tiny_grad.npz")) // 1024, "KB")
+        return
     out = {}
     # 1. tiny layered, F-cycles: converged fields + mode=2 adjoint/gradient
     out["tiny_layered"] = case(W.tiny_layered(), ["tol=1e-10", "ncycle=60"], adjoint=1)

@@ -188,3 +188,31 @@ def test_nonfinite_rhs_reports_status(golden):
     s = _solver(g, ncycle=10, tol=1e-8)
     x, h, st = s.solve(b[None])
     assert st[0]["status"] == "nonfinite"
+
+
+@gpu
+def test_stored_line_factors_give_the_same_iterates(golden):
+    """Mixed cycles with the line factors kept from set-up (the default) and
+    factored in every sweep: the same operations in the same order (the
+    compiler may fuse multiply-adds differently in the two kernels, so
+    roundoff, amplified in the air layer's curl-free E, is all that differs)."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"]])
+    oms = np.array([om, om, 0.5 * om], np.float32)
+    out = {}
+    for lf in (1, 0):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
+                     op=np.zeros(3, np.int32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=6, tol=0.0,
+                                       sigma_floor=2e-4, line_factors=lf))
+        x, h, st = s.solve(bs)
+        out[lf] = (x, h, [q["cycles"] for q in st], s.device_bytes)
+        s.close()
+    assert out[1][3] > out[0][3]          # the factors are held
+    assert out[1][2] == out[0][2] == [6, 6, 6]
+    sea = below_sea_mask(n, g["x3"])
+    for r in range(3):
+        assert rel_err(out[1][0][r], out[0][0][r], sea) < 1e-6
+        assert rel_err(out[1][1][r], out[0][1][r]) < 1e-6
