@@ -338,6 +338,10 @@ def main():
     traffic = ncu_traffic()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
+            # the DRAM bytes the sweep really moves (ncu, scaled to 25 RHS) per
+            # second: what the kernels achieve against the memory system
+            "traffic_GBps": round(traffic / (ms * 1e-3) / 1e9, 1) if traffic else None,
+            "traffic_frac": round(traffic / (ms * 1e-3) / 1e9 / peak, 4) if traffic else None,
             "kernel": "level-0 line sweep along x, 4 colours x (k_line_rhs, k_line_subst, "
                       "k_line_apply_rb)<float> with stored line factors, 25 RHS",
             "ms_per_sweep": round(ms, 4), "ms_per_sweep_xyz": ms_dir, "launches_per_sweep": nl,
@@ -351,7 +355,9 @@ def main():
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record()
-        sv = make_solver(w, G.PREC_MIXED, a.tol)
+        sv = make_solver(w, G.PREC_MIXED, a.tol, krylov=a.krylov)
+        if W is not None:
+            sv.set_learned(W)  # the weights trained above, as a caller would reuse them
         _, _, (hb, db) = sv.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
         sv.close()
         t1.record()
