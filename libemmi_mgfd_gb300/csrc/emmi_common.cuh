@@ -134,6 +134,11 @@ template <typename T> struct EdgeCoef {
   T c[12];
 };
 
+// a / b: the hardware's fast single-precision division for the complex64
+// operator (the preconditioner: 2 ulp are immaterial there), IEEE for FP64
+__device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
+
 // P[3]: node indices of the edge; strides of the cell array; G geometry.
 template <typename T, int C>
 __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const T* __restrict__ sigC,
@@ -155,16 +160,16 @@ __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const 
   const T dc = ldro(G.ds(C) + a);
   const T dpp = ldro(G.ds(p) + b), dpm = ldro(G.ds(p) + b - 1);
   const T dqp = ldro(G.ds(q) + g), dqm = ldro(G.ds(q) + g - 1);
-  const T kpp = m1 / (dpp * dpp), kpm = m2 / (dpm * dpm);
-  const T kqp = m3 / (dqp * dqp), kqm = m4 / (dqm * dqm);
+  const T kpp = qdiv(m1, dpp * dpp), kpm = qdiv(m2, dpm * dpm);
+  const T kqp = qdiv(m3, dqp * dqp), kqm = qdiv(m4, dqm * dqm);
   e.dre = (kpp + kpm) + (kqp + kqm);
   e.dim = -wmu * s;
   e.c[0] = -kpp;
   e.c[1] = -kpm;
   e.c[2] = -kqp;
   e.c[3] = -kqm;
-  const T xp = m1 / (dc * dpp), xm = m2 / (dc * dpm);
-  const T yp = m3 / (dc * dqp), ym = m4 / (dc * dqm);
+  const T xp = qdiv(m1, dc * dpp), xm = qdiv(m2, dc * dpm);
+  const T yp = qdiv(m3, dc * dqp), ym = qdiv(m4, dc * dqm);
   e.c[4] = xp;
   e.c[5] = -xp;
   e.c[6] = -xm;
@@ -182,6 +187,17 @@ __device__ __forceinline__ long nbr_slot_delta(int k, const long ss[3], long S) 
   const NbrOff o = nbr_off(C, k);
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
   return (long)o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
+}
+
+// slot index -> node indices with 32-bit arithmetic (a level holds fewer
+// than 2^31 slots per right-hand side): one division and one modulo fewer
+// than the 64-bit decomposition, which dominated the index work
+__device__ __forceinline__ void slot_nodes(long s, int n0, int n1, int P[3]) {
+  const unsigned u = (unsigned)s, a = (unsigned)n0, b = (unsigned)n1;
+  const unsigned t = u / a;
+  P[0] = (int)(u - t * a);
+  P[1] = (int)(t % b);
+  P[2] = (int)(t / b);
 }
 
 // (A u) of the edge equation of component C at slot s, and its coefficients

@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
   double acc = 0.0;
   if (s < L.S) {
     const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
-    const int P[3] = {(int)(s % n0), (int)((s / n0) % n1), (int)(s / ((long)n0 * n1))};
+    int P[3];
+    slot_nodes(s, n0, n1, P);
     const long ss[3] = {1, (long)n0, (long)n0 * n1};
     const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
     const C_t<T>* f = L.f ? L.f + (long)rhs * 3 * L.S : nullptr;
@@ -148,6 +149,122 @@ void launch_residual(const LevelView<T>& L, C_t<TO>* rout, double* norm2, cudaSt
   dim3 grid((unsigned)((L.S + 255) / 256), L.nrhs);
   k_residual<T, TO><<<grid, 256, 0, st>>>(L, rout, norm2);
 }
+
+// ------------------------------------------------------------ stored FP64 coefficients
+// The FP64 refinement residual of the mixed solver recomputes, per edge, 8
+// coupling values with 8 divisions at GB300's FP64 rate.  They depend on the
+// operator only (the imaginary diagonal on omega too, as -omega*mu0 * sbar),
+// so they are stored once per operator: planes [op][10][3][S] of kpp, kpm,
+// kqp, kqm (c[0..3]), xp, xm, yp, ym (c[4], c[7], c[8], c[11]), the real
+// diagonal and sbar, taken from edge_coef itself.  The residual then applies
+// them in edge_coef/apply_row's order: the same result, bit for bit.
+constexpr int kCoef = 10;
+
+template <int C>
+__device__ __forceinline__ void store_coef(const LevelView<double>& L, const double* cells,
+                                           const Geo<double>& G, const int P[3], long s,
+                                           double* __restrict__ out) {
+  EdgeCoef<double> e;
+  // omega*mu0 = -1 gives dim = -(-1)*sbar = sbar exactly
+  edge_coef<double, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, -1.0, e);
+  const long n3s = 3 * L.S, o = (long)C * L.S + s;
+  const double v[kCoef] = {e.c[0], e.c[1], e.c[2], e.c[3], e.c[4], e.c[7], e.c[8], e.c[11],
+                           e.dre, e.dim};
+#pragma unroll
+  for (int k = 0; k < kCoef; k++) out[k * n3s + o] = v[k];
+}
+
+// blockIdx.y = operator
+__global__ void __launch_bounds__(256) k_coef64(LevelView<double> L, double* __restrict__ coef) {
+  const int op = blockIdx.y;
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= L.S) return;
+  const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
+  int P[3];
+    slot_nodes(s, n0, n1, P);
+  const double* cells = L.cells + (long)op * 4 * L.ncell;
+  const Geo<double> G{L.geo + (long)op * L.gstride, L.gmax1};
+  double* out = coef + (long)op * kCoef * 3 * L.S;
+  if (is_unknown<0>(L.n, P)) store_coef<0>(L, cells, G, P, s, out);
+  if (is_unknown<1>(L.n, P)) store_coef<1>(L, cells, G, P, s, out);
+  if (is_unknown<2>(L.n, P)) store_coef<2>(L, cells, G, P, s, out);
+}
+
+template <typename TO, int C>
+__device__ __forceinline__ double residual_comp_coef(const LevelView<double>& L,
+                                                     const double2* u, const double2* f,
+                                                     const double* __restrict__ cf, double wmu,
+                                                     const int P[3], long s, const long ss[3],
+                                                     C_t<TO>* rout) {
+  double2 r = f ? f[(long)C * L.S + s] : make_double2(0.0, 0.0);
+  if (is_unknown<C>(L.n, P)) {
+    const long n3s = 3 * L.S, o = (long)C * L.S + s;
+    double k8[kCoef];
+#pragma unroll
+    for (int k = 0; k < kCoef; k++) k8[k] = ldro(cf + k * n3s + o);
+    const double c[12] = {k8[0], k8[1], k8[2], k8[3], k8[4], -k8[4], -k8[5], k8[5],
+                          k8[6], -k8[6], -k8[7], k8[7]};
+    const double dre = k8[8], dim = -wmu * k8[9];
+    const double2 uc = ldro(u + o);
+    double ar = dre * uc.x - dim * uc.y;
+    double ai = dre * uc.y + dim * uc.x;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const double2 v = ldro(u + s + nbr_slot_delta<C>(k, ss, L.S));
+      ar += c[k] * v.x;
+      ai += c[k] * v.y;
+    }
+    r = csub<double>(r, mk<double>(ar, ai));
+  }
+  if (rout) rout[(long)C * L.S + s] = mk<TO>((TO)r.x, (TO)r.y);
+  return r.x * r.x + r.y * r.y;
+}
+
+template <typename TO>
+__global__ void __launch_bounds__(256) k_residual_coef(LevelView<double> L,
+                                                       const double* __restrict__ coef,
+                                                       C_t<TO>* __restrict__ rout,
+                                                       double* __restrict__ norm2) {
+  const int rhs = blockIdx.y;
+  if (L.active && !L.active[rhs]) return;
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (s < L.S) {
+    const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
+    int P[3];
+    slot_nodes(s, n0, n1, P);
+    const long ss[3] = {1, (long)n0, (long)n0 * n1};
+    const double2* u = L.u + (long)rhs * 3 * L.S;
+    const double2* f = L.f ? L.f + (long)rhs * 3 * L.S : nullptr;
+    const double* cf = coef + (long)op_of(L, rhs) * kCoef * 3 * L.S;
+    const double wmu = L.wmu[rhs];
+    C_t<TO>* ro = rout ? rout + (long)rhs * 3 * L.S : nullptr;
+    acc += residual_comp_coef<TO, 0>(L, u, f, cf, wmu, P, s, ss, ro);
+    acc += residual_comp_coef<TO, 1>(L, u, f, cf, wmu, P, s, ss, ro);
+    acc += residual_comp_coef<TO, 2>(L, u, f, cf, wmu, P, s, ss, ro);
+  }
+  if (norm2) block_add(acc, norm2 + rhs);
+}
+
+long coef64_elems(const int n[3]) {
+  return (long)kCoef * 3 * (n[0] + 1) * (n[1] + 1) * (n[2] + 1);
+}
+
+void launch_coef64(const LevelView<double>& L, double* coef, cudaStream_t st) {
+  dim3 grid((unsigned)((L.S + 255) / 256), L.nrhs);
+  k_coef64<<<grid, 256, 0, st>>>(L, coef);
+}
+
+template <typename TO>
+void launch_residual_coef(const LevelView<double>& L, const double* coef, C_t<TO>* rout,
+                          double* norm2, cudaStream_t st) {
+  dim3 grid((unsigned)((L.S + 255) / 256), L.nrhs);
+  k_residual_coef<TO><<<grid, 256, 0, st>>>(L, coef, rout, norm2);
+}
+template void launch_residual_coef<float>(const LevelView<double>&, const double*, C_t<float>*,
+                                          double*, cudaStream_t);
+template void launch_residual_coef<double>(const LevelView<double>&, const double*,
+                                           C_t<double>*, double*, cudaStream_t);
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_norm(const C_t<T>* __restrict__ v, long n, const int* active,
@@ -249,11 +366,14 @@ template <int D>
 __device__ __forceinline__ bool line_item(const LineGeom& g, long id, long& l, int& s) {
   if (id >= g.nl * g.nd) return false;
   if (D == 0) {  // rows of an x-line are contiguous in memory
-    l = id / g.nd;
-    s = 1 + (int)(id % g.nd);
+    const unsigned u = (unsigned)id, nd = (unsigned)g.nd;
+    l = u / nd;
+    s = 1 + (int)(u - (unsigned)l * nd);
   } else {  // neighbouring lines (consecutive i) are contiguous
-    l = id % g.nl;
-    s = 1 + (int)(id / g.nl);
+    const unsigned u = (unsigned)id, nl = (unsigned)g.nl;
+    const unsigned q = u / nl;
+    l = u - q * nl;
+    s = 1 + (int)q;
   }
   return true;
 }
@@ -319,7 +439,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(L
   long l;
   int s;
   if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
-  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
   const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
@@ -353,13 +474,14 @@ __global__ void __launch_bounds__(256) k_line_assemble_rows(LevelView<T> L, int 
   const LineGeom g = line_geom<D>(L.n, pa, pb);
   const long items = g.nl * g.nd;
   const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const int rt = (int)(id / items);
+  const int rt = (int)((unsigned)id / (unsigned)items);
   if (rt >= 5) return;
   long l;
   int s;
   if (!line_item<D>(g, id - rt * items, l, s)) return;
   if (rt > 0 && s == g.nd) return;  // the last node carries only its E_D row
-  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
   const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
@@ -527,7 +649,8 @@ __global__ void __launch_bounds__(256) k_line_apply(LevelView<T> L, int pa, int 
   long l;
   int s;
   if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
-  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   using V = typename Vec16<T>::V;
   C_t<T>* u = L.u + (long)rhs * 3 * L.S;
   const V* base = reinterpret_cast<const V*>(buf) + (long)rhs * g.m * kPlanes<T> * g.nl + l;
@@ -583,7 +706,7 @@ __global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb
   long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
   int rt = 0;
   if (D == 0) {
-    rt = (int)(id / items);
+    rt = (int)((unsigned)id / (unsigned)items);
     if (rt >= 5) return;
     id -= rt * items;
   }
@@ -591,7 +714,8 @@ __global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb
   int s;
   if (!line_item<D>(g, id, l, s)) return;
   if (D == 0 && rt > 0 && s == g.nd) return;
-  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
   const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
@@ -818,7 +942,8 @@ __global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, i
   long l;
   int s;
   if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
-  const int ta = g.fa + 2 * (int)(l % g.la), tb = g.fb + 2 * (int)(l / g.la);
+  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   C_t<T>* u = L.u + (long)rhs * 3 * L.S;
   const C_t<T>* x = rb + (long)rhs * g.m * g.nl + l;
   const int r0 = 5 * (s - 1);
@@ -1105,7 +1230,8 @@ __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C
   if (s >= Cc.S) return;
   const int sc[3] = {sc0, sc1, sc2};
   const int n0 = Cc.n[0] + 1, n1 = Cc.n[1] + 1;
-  const int Cn[3] = {(int)(s % n0), (int)((s / n0) % n1), (int)(s / ((long)n0 * n1))};
+  int Cn[3];
+  slot_nodes(s, n0, n1, Cn);
   const C_t<T>* rf = F.r + (long)rhs * 3 * F.S;
   C_t<T>* fc = Cc.f + (long)rhs * 3 * Cc.S;
   C_t<T>* uc = Cc.u + (long)rhs * 3 * Cc.S;
@@ -1168,7 +1294,8 @@ __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> Cc
   if (s >= F.S) return;
   const int sc[3] = {sc0, sc1, sc2};
   const int n0 = F.n[0] + 1, n1 = F.n[1] + 1;
-  const int P[3] = {(int)(s % n0), (int)((s / n0) % n1), (int)(s / ((long)n0 * n1))};
+  int P[3];
+    slot_nodes(s, n0, n1, P);
   C_t<T>* uf = F.u + (long)rhs * 3 * F.S;
   const C_t<T>* uc = Cc.u + (long)rhs * 3 * Cc.S;
   const Geo<T> Gf{F.geo + (long)op_of(F, rhs) * F.gstride, F.gmax1};

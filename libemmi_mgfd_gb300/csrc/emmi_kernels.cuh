@@ -11,6 +11,15 @@ void init_line_kernels();
 template <typename T, typename TO>
 void launch_residual(const LevelView<T>& L, C_t<TO>* rout, double* norm2, cudaStream_t st);
 
+// stored FP64 edge coefficients of level-0 operators (L.nrhs operators,
+// L.op unused): coef64_elems doubles per operator; launch_residual_coef is
+// launch_residual<double, TO> reading them, bit for bit the same result
+long coef64_elems(const int n[3]);
+void launch_coef64(const LevelView<double>& L, double* coef, cudaStream_t st);
+template <typename TO>
+void launch_residual_coef(const LevelView<double>& L, const double* coef, C_t<TO>* rout,
+                          double* norm2, cudaStream_t st);
+
 // r = f - A u on level L but only norm (no store)
 template <typename T>
 void launch_norm(const C_t<T>* v, long n3s, int nrhs, const int* active, double* norm2,

@@ -322,7 +322,7 @@ int krylov_solve(emmi_solver* s, std::vector<int>& cycles, std::vector<int>& sta
     V.f = s->f64[0];
     V.active = mask;
     CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), st));
-    launch_residual<double, double>(V, s->kv, s->d_norm64, st);
+    true_residual64<double>(s, V, s->kv, s->d_norm64);
     s->last_launches++;
     CK(cudaMemcpyAsync(nrm.data(), s->d_norm64, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -372,7 +372,7 @@ int krylov_solve(emmi_solver* s, std::vector<int>& cycles, std::vector<int>& sta
     V.u = s->kt;
     V.f = nullptr;
     V.active = s->d_active;
-    launch_residual<double, double>(V, s->kw, nullptr, st);
+    true_residual64<double>(s, V, s->kw, nullptr);
     // classical Gram-Schmidt against v_0..v_j, twice (the second pass
     // restores the orthogonality the first loses when A M^-1 has clustered
     // eigenvalues), then |v_{j+1}|

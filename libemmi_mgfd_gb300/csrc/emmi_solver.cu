@@ -518,6 +518,28 @@ static int build_line_factors(emmi_solver* s) {
   return EMMI_OK;
 }
 
+// Stored FP64 coefficients of the level-0 true operators for the mixed
+// solver's refinement residual, when they fit in half of the free device
+// memory (else the residual computes them, as the FP64 solver does)
+static int build_coef64(emmi_solver* s) {
+  const HLev& L0 = s->hier[0][0];
+  const size_t bytes = (size_t)s->nop * coef64_elems(L0.n) * sizeof(double);
+  size_t freeb = 0, totb = 0;
+  CK(cudaMemGetInfo(&freeb, &totb));
+  if (bytes > freeb / 2) return EMMI_OK;
+  int rc;
+  if ((rc = s->alloc((void**)&s->d_coef64, bytes)) != EMMI_OK) return rc;
+  CK(cudaMemsetAsync(s->d_coef64, 0, bytes, s->st));
+  LevelView<double> V = s->view<double>(0, 0);
+  V.nrhs = s->nop;
+  V.op = nullptr;
+  V.active = nullptr;
+  launch_coef64(V, s->d_coef64, s->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s->st));
+  return EMMI_OK;
+}
+
 // ============================================================ C ABI
 extern "C" {
 
@@ -826,6 +848,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     TRY(s->alloc(&s->scratch, s->scratch_bytes));
     if (mixed && s->opt.krylov > 0) TRY(krylov_alloc(s));
     if (mixed && s->opt.line_factors) TRY(build_line_factors(s));
+    if (mixed) TRY(build_coef64(s));
   }
 
   // ---- graphs
@@ -971,7 +994,7 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
           W.f = s->f64[0];
           W.active = s->d_refine;
           CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
-          launch_residual<double, float>(W, s->f32[0], s->d_norm64, s->st);
+          true_residual64<float>(s, W, s->f32[0], s->d_norm64);
           k_zero_masked<<<g, 256, 0, s->st>>>(s->u32[0], n3s, s->d_refine);
           s->last_launches += 3;
           if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
@@ -1038,7 +1061,7 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
       W.f = s->f64[0];
       W.active = s->d_refine;
       CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
-      launch_residual<double, float>(W, s->f32[0], s->d_norm64, s->st);
+      true_residual64<float>(s, W, s->f32[0], s->d_norm64);
       s->last_launches += 2;
       if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
       for (int r = 0; r < nrhs; r++)

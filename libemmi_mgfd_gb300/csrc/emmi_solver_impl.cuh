@@ -83,6 +83,10 @@ struct emmi_solver {
   size_t fac_bytes = 0;
   long fac_off[3][emmi::kMaxLev][3][4];
 
+  // stored FP64 edge coefficients of the level-0 true operators (MIXED):
+  // the refinement residual reads them instead of recomputing (null: off)
+  double* d_coef64 = nullptr;
+
   // FGMRES (MIXED, opt.krylov > 0): basis kv [m+1][nrhs][3S] FP64,
   // preconditioned directions kz [m][nrhs][3S] complex64, FP64 temporaries
   // kt (-z) and kw (A z) [nrhs][3S]; per RHS: Hessenberg column d_kh
@@ -126,6 +130,17 @@ struct emmi_solver {
 
 // one part of a cycle on hierarchy h (graph launch or direct emission)
 int run_part(emmi_solver* s, int h, int part);
+
+// FP64 r = f - A u on level 0 with the true operator (V a level-0 FP64
+// view): from the stored coefficients when the solver keeps them
+template <typename TO>
+inline void true_residual64(emmi_solver* s, const emmi::LevelView<double>& V, emmi::C_t<TO>* rout,
+                            double* norm2) {
+  if (s->d_coef64)
+    emmi::launch_residual_coef<TO>(V, s->d_coef64, rout, norm2, s->st);
+  else
+    emmi::launch_residual<double, TO>(V, rout, norm2, s->st);
+}
 
 namespace emmi {
 // FGMRES workspace for opt.krylov > 0 (called by emmi_solver_create)
