@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--profile", action="store_true",
                    help="one shot: a short solve, then one level-0 line sweep inside the NVTX "
                         "range emmi_profile (for ncu --nvtx-include emmi_profile/)")
+    p.add_argument("--profile-learned", action="store_true",
+                   help="with --profile: one application of the learned correction (seeded "
+                        "weights, seeded level-0 iterates) instead of the line sweep")
     return p.parse_args()
 
 
@@ -257,9 +260,20 @@ def main():
     if a.profile:
         sp = make_solver(w, G.PREC_MIXED, a.tol)
         sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
-        torch.cuda.nvtx.range_push("emmi_profile")
-        sp.time_smoother(0, reps=1)
-        torch.cuda.nvtx.range_pop()
+        if a.profile_learned:
+            rng = np.random.default_rng(11)
+            sp.set_learned((0.05 * rng.standard_normal(2 * 27 * 64)).astype(np.float32))
+            shape = (nrhs, 3 * sp.nslots)
+            f = torch.complex(torch.randn(shape, device="cuda"), torch.randn(shape, device="cuda"))
+            u = torch.zeros_like(f)
+            sp.learned_apply(f, u)  # warm-up outside the range
+            torch.cuda.nvtx.range_push("emmi_profile")
+            sp.learned_apply(f, u)
+            torch.cuda.nvtx.range_pop()
+        else:
+            torch.cuda.nvtx.range_push("emmi_profile")
+            sp.time_smoother(0, reps=1)
+            torch.cuda.nvtx.range_pop()
         sp.close()
         print(json.dumps({"profile": "done", "n": a.n, "nrhs": nrhs}))
         return

@@ -128,9 +128,12 @@ const char *emmi_last_error(void);
 
 /* ---- learned correction (no counterpart in the reference) -------------- */
 /* A small linear 3x3x3 convolutional network (8 -> 8 -> 8 channels, bf16
- * tensor-core forward, 2 x 1728 fp32 weights [layer][tap][cin][cout], tap =
- * (dk+1)*9+(dj+1)*3+(di+1)) that corrects the level-0 complex64 iterate after
+ * tcgen05 tensor-core forward, 2 x 1728 fp32 weights [layer][tap][cin][cout],
+ * tap = (dk+1)*9+(dj+1)*3+(di+1); the hidden layer is zero on the last slot
+ * plane of each direction) that corrects the level-0 complex64 iterate after
  * every cycle of a MIXED solver: u += N(D^-1 (f - A u)) on unknown edges.
+ * Levels whose rows are too wide for the convolution's shared-memory window
+ * (more than about 1600 slots) are refused with EMMI_EINVAL.
  * Training minimises sum_b |r_b - A N(D^-1 r_b)|^2 / |r_b|^2 over residual
  * samples r_b of plain cycles.  A RHS whose FP64 residual does not halve
  * between refinements (restarts with krylov) with the correction on falls
@@ -155,6 +158,10 @@ int emmi_learned_grad(emmi_solver *s, const float *W, float *loss,
                       float *grad);
 /* use W in the following solves; W = NULL switches the correction off */
 int emmi_learned_set(emmi_solver *s, const float *W);
+/* One application of the correction set by emmi_learned_set to complex64
+ * level-0 iterates: u += N(D^-1 (f - A u)), f and u device arrays
+ * [nrhs][3][S] of the solver's operators (synchronises the stream). */
+int emmi_learned_apply(emmi_solver *s, const void *f, void *u);
 
 /* ---- survey: injection, extraction, gradient (src/inject_extract.c,
  *      src/build_gradient.c) ------------------------------------------- */

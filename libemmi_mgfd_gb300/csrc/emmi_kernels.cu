@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_coef64(LevelView<double> L, double* __r
   if (s >= L.S) return;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   int P[3];
-    slot_nodes(s, n0, n1, P);
+  slot_nodes(s, n0, n1, P);
   const double* cells = L.cells + (long)op * 4 * L.ncell;
   const Geo<double> G{L.geo + (long)op * L.gstride, L.gmax1};
   double* out = coef + (long)op * kCoef * 3 * L.S;

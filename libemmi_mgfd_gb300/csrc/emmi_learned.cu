@@ -11,24 +11,30 @@
 // complex64 iterate divided by the diagonal of A edge by edge, as 8 channels
 // per slot (Ex, Ey, Ez real/imaginary + 2 zero channels) on the
 // (n1+1)(n2+1)(n3+1) slot grid; two bias-free linear 3x3x3 convolutions
-// 8 -> 8 -> 8 channels (hidden layer bf16); the first 6 output channels are
-// the correction, added on unknown edges only.  A linear, bias-free network
-// keeps the corrected cycle a fixed linear preconditioner (scale-equivariant),
-// so stationary refinement and FGMRES both stay valid.
+// 8 -> 8 -> 8 channels with zero padding; the hidden layer is rounded to
+// bf16 and is zero on the last slot plane of each direction (i = n1, j = n2,
+// k = n3), where no component has an unknown edge; the first 6 output
+// channels are the correction, added on unknown edges only.  A linear,
+// bias-free network keeps the corrected cycle a fixed linear preconditioner
+// (scale-equivariant), so stationary refinement and FGMRES both stay valid.
 //
-// Forward convolutions run on the tensor cores as an implicit GEMM:
-// M = 16 consecutive slots along i, N = 8 output channels, K = tap x channel
-// (two taps per k16 step, 14 steps, the 28th tap zero), bf16 operands, fp32
-// accumulation (mma.sync m16n8k16; the channel count of 8 is below the
-// 64/128-row tiles tcgen05 issues, and the whole network is ~1 % of a cycle).
-// Training: loss = sum_b |r_b - A c_b|^2 / |r_b|^2 over residual samples r_b
-// (c_b the masked correction), gradients by fp32 CUDA-core kernels.
+// The convolutions run on the fifth-generation tensor cores (tcgen05.mma,
+// bf16 operands from shared memory, fp32 accumulators in tensor memory) as
+// an implicit GEMM over the flattened slot index s = i + X j + X Y k: tap
+// (di, dj, dk) reads slot s + di + X dj + X Y dk.  On the flattened index a
+// tap that leaves the grid lands on the last plane of a lower direction (or
+// on the previous right-hand side's last plane, or a zero guard), and both
+// layer inputs are zero there, so the flattened convolution equals the
+// zero-padded one on every slot whose output is used.  Training: loss =
+// sum_b |r_b - A c_b|^2 / |r_b|^2 over residual samples r_b (c_b the masked
+// correction), gradients by fp32 CUDA-core kernels.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -40,7 +46,7 @@ namespace {
 
 constexpr int kCh = 8;
 constexpr int kTaps = 27;
-constexpr int kKSteps = 14;
+constexpr int kTcInstr = 15;  // tcgen05.mma per output tile
 constexpr int kWLayer = kTaps * kCh * kCh;  // [tap][cin][cout]
 
 // tap t = (dk+1)*9 + (dj+1)*3 + (di+1)
@@ -71,27 +77,33 @@ __device__ __forceinline__ bool unknown_any(int c, const int n[3], int i, int j,
 }
 
 // ---------------------------------------------------------------- weights
-// B fragments of mma.m16n8k16 (k x n = 16 x 8): lane (g = lane/4, t4 = lane%4)
-// holds k = 2*t4, 2*t4+1 (reg 0) and k = 2*t4+8, +9 (reg 1) of column n = g.
-// Here k in [0,8) is tap 2*ks, channels 0..7; k in [8,16) tap 2*ks+1.
-__global__ void k_ls_pack(const float* __restrict__ W, uint32_t* __restrict__ Wp) {
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;  // [layer][ks][lane]
-  if (id >= 2 * kKSteps * 32) return;
-  const int lane = id % 32, ks = (id / 32) % kKSteps, layer = id / (32 * kKSteps);
-  const int g = lane >> 2, t4 = lane & 3;
+// B operands of the tensor-core convolution, one 16 x 16 bf16 matrix per
+// instruction (N = 16 output columns, 8 of them zero; K = 16 = two taps x 8
+// input channels), K-major without swizzle: the 8 x 8 core matrix (n-group
+// ng, k-group kc) at byte 256 kc + 128 ng, row n % 8 at 16 bytes, element
+// k % 8 at 2 bytes.  Instruction q covers plane dk = q / 5 - 1 and the tap
+// pair 2 (q % 5), 2 (q % 5) + 1 of that plane's 9 taps (raster (dj, di));
+// the fifth pair holds the ninth tap alone (its second half zero).
+__global__ void k_ls_pack(const float* __restrict__ W, uint4* __restrict__ Wt) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;  // [layer][q][kc][ng][n8]
+  if (id >= 2 * kTcInstr * 32) return;
+  const int n8 = id & 7, ng = (id >> 3) & 1, kc = (id >> 4) & 1, q = (id >> 5) % kTcInstr,
+            layer = id / (32 * kTcInstr);
+  const int dk = q / 5 - 1, pi = q % 5;
+  const int r = 2 * pi + kc;  // tap of this k-group within the plane's raster
+  const int n = 8 * ng + n8;
   const float* w = W + layer * kWLayer;
-  uint32_t r[2];
-  for (int h = 0; h < 2; h++) {
-    const int t = 2 * ks + h;
+  uint32_t v[4];
+  for (int e = 0; e < 4; e++) {
     float lo = 0.f, hi = 0.f;
-    if (t < kTaps) {
-      lo = w[(t * kCh + 2 * t4) * kCh + g];
-      hi = w[(t * kCh + 2 * t4 + 1) * kCh + g];
+    if (n < kCh && r < 9) {
+      const int t = (dk + 1) * 9 + r;
+      lo = w[(t * kCh + 2 * e) * kCh + n];
+      hi = w[(t * kCh + 2 * e + 1) * kCh + n];
     }
-    r[h] = pack_bf16x2(lo, hi);
+    v[e] = pack_bf16x2(lo, hi);
   }
-  Wp[2 * id] = r[0];
-  Wp[2 * id + 1] = r[1];
+  Wt[id] = make_uint4(v[0], v[1], v[2], v[3]);
 }
 
 // ---------------------------------------------------------------- input
@@ -104,7 +116,8 @@ __global__ void __launch_bounds__(256) k_ls_input(LevelView<float> L, const floa
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= L.S) return;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
-  const int P[3] = {(int)(s % n0), (int)((s / n0) % n1), (int)(s / ((long)n0 * n1))};
+  int P[3];
+  slot_nodes(s, n0, n1, P);
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
   const float2* u = L.u + (long)b * 3 * L.S;
   const float2* f = L.f ? L.f + (long)b * 3 * L.S : nullptr;
@@ -126,9 +139,9 @@ __global__ void __launch_bounds__(256) k_ls_input(LevelView<float> L, const floa
       r = make_float2(fv.x - au.x, fv.y - au.y);
     }
     // z = r / d = r conj(d) / |d|^2
-    const float d2 = e.dre * e.dre + e.dim * e.dim;
-    const float zr = (r.x * e.dre + r.y * e.dim) / d2;
-    const float zi = (r.y * e.dre - r.x * e.dim) / d2;
+    const float inv = 1.f / (e.dre * e.dre + e.dim * e.dim);
+    const float zr = (r.x * e.dre + r.y * e.dim) * inv;
+    const float zi = (r.y * e.dre - r.x * e.dim) * inv;
     out[C] = pack_bf16x2(zr, zi);
   };
   one(std::integral_constant<int, 0>());
@@ -138,113 +151,303 @@ __global__ void __launch_bounds__(256) k_ls_input(LevelView<float> L, const floa
 }
 
 // ---------------------------------------------------------------- conv
-// One 3x3x3 convolution, 8 -> 8 channels, on the tensor cores.  A block of
-// 4 warps owns a brick of 48 x 2 x 2 slots (i, j, k): it stages the brick
-// and its one-slot halo (50 x 4 x 4 slots x 16 bytes) in shared memory with
-// coalesced loads, then each warp computes 3 of the brick's 12 m-tiles
-// (16 consecutive slots along i) with A fragments read from shared memory
-// (8 consecutive slots x 4 words per load: conflict-free).
-//   MODE 0: out = hidden layer, bf16 [b][S][8]
+// PTX wrappers: mbarriers, the bulk copy engine, tensor memory, tcgen05.
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ uint32_t mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok;
+}
+// a wait that gives up after about a second (false): the caller records the
+// failure and leaves without touching the data
+constexpr long long kWaitCycles = 2000000000LL;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::
+          "r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor: D f32, A and B bf16, both K-major, N = 16, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) |
+                            ((128u >> 4) << 24);
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                   bar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_load8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// One 3x3x3 convolution, 8 -> 8 channels, bf16 slots [b][S] (16 bytes per
+// slot) with kTcGuard(X, Y) zero slots before the first and after the last
+// right-hand side.  A CTA of 4 warps owns one column of 128 consecutive
+// in-plane slots (p = i + X j in [128 col, 128 col + 128)) and walks the
+// planes k of one chunk; for plane k the output tile is D[m][n] =
+// sum_taps X[s_m + off(tap)] W_tap, 15 tcgen05.mma (M = 128 slots, N = 16,
+// K = 16) into one of two tensor-memory accumulators, so that the MMAs of
+// plane k run while the epilogue of plane k-1 reads the other one back.
+// Each plane's window (slots 128 col - X - 1 ... 128 col + 127 + X + 2 of
+// that plane, contiguous) comes in by one bulk copy, two planes ahead, into
+// a ring of 5 windows; the window serves as the A operand of the plane's
+// three dk roles directly: tap (di, dj) of a window is the 128-row matrix
+// starting X + 1 + X dj + di slots in (rows 16 bytes apart, 8 channels each
+// = one core-matrix row).
+//   MODE 0: hidden layer, bf16 [b][S] (guarded layout), zero on the planes
+//           i = X-1, j = Y-1, k = Z-1
 //   MODE 1: u += channels 0..5 on unknown edges (deployment)
 //   MODE 2: c = channels 0..5 on unknown edges, 0 elsewhere ([b][3][S])
+// Plane k = Z-1 holds no unknown edge: it is never computed (MODE 0 and 2
+// write its zeros).  Waits are bounded; a CTA that gives up sets *err,
+// drains its copies and frees its tensor memory.
 struct ConvArgs {
   int n[3];      // cells of the level
   int X, Y, Z;   // slots per direction (n+1)
   long S;
-  int tiles;     // bricks per RHS
+  int XY;        // slots per plane
+  int ncol;      // 128-slot columns per plane
+  int nchunk;    // plane chunks per column
+  int W;         // window slots: 128 + 2X + 3
+  int wbytes;    // window stride in shared memory (16 W rounded up to 128)
   const int* mask;
 };
 
-constexpr int kBI = 48, kBJ = 2, kBK = 2;
-constexpr int kHI = kBI + 2, kHJ = kBJ + 2, kHK = kBK + 2;
+constexpr int kTcRing = 5;
+constexpr int kTcPlanes = 32;  // planes per chunk
+constexpr int kTcCols = 32;    // tensor-memory columns allocated (16 used)
+// dynamic shared memory a CTA may ask for (227 KB less the static part)
+constexpr int kConvSmemMax = 227 * 1024 - 1024;
+__host__ __device__ inline long kTcGuard(int X, int Y) { return (long)X * Y + X + 129; }
+inline size_t conv_smem(const ConvArgs& a) {
+  return (size_t)kTcInstr * 512 + (size_t)kTcRing * a.wbytes;
+}
 
 template <int MODE>
-__global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint32_t* __restrict__ in,
-                                                 const uint32_t* __restrict__ Wp,
-                                                 uint32_t* __restrict__ hid,
-                                                 float2* __restrict__ out) {
-  __shared__ uint4 halo[kHK * kHJ * kHI];
+__global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __restrict__ in,
+                                                 const uint4* __restrict__ Wt,
+                                                 uint4* __restrict__ hid,
+                                                 float2* __restrict__ out, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char dsm[];
+  __shared__ __align__(8) uint64_t bar_full[kTcRing];
+  __shared__ __align__(8) uint64_t bar_mma[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ int failed;
   const int b = blockIdx.y;
   if (a.mask && !a.mask[b]) return;
-  const int nbi = (a.X + kBI - 1) / kBI, nbj = (a.Y + kBJ - 1) / kBJ;
-  const int brick = blockIdx.x;
-  const int bi0 = (brick % nbi) * kBI;
-  const int bj0 = ((brick / nbi) % nbj) * kBJ;
-  const int bk0 = (brick / (nbi * nbj)) * kBK;
-  const uint4* inb = reinterpret_cast<const uint4*>(in) + (long)b * a.S;
-  for (int q = threadIdx.x; q < kHK * kHJ * kHI; q += blockDim.x) {
-    const int hi = q % kHI, hj = (q / kHI) % kHJ, hk = q / (kHI * kHJ);
-    const int i = bi0 + hi - 1, j = bj0 + hj - 1, k = bk0 + hk - 1;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (i >= 0 && i < a.X && j >= 0 && j < a.Y && k >= 0 && k < a.Z)
-      v = inb[((long)k * a.Y + j) * a.X + i];
-    halo[q] = v;
+  if (*(volatile int*)err) return;  // an earlier CTA gave up: the launch has failed
+  const int col = blockIdx.x % a.ncol, chunk = blockIdx.x / a.ncol;
+  const int k0 = chunk * kTcPlanes;
+  const int k1 = min(k0 + kTcPlanes, a.Z - 1);  // planes [k0, k1) are computed
+  const int tid = threadIdx.x, warp = tid >> 5;
+  uint4* sB = reinterpret_cast<uint4*>(dsm);
+  unsigned char* ring = dsm + kTcInstr * 512;
+  const uint4* inb = in + (long)b * a.S;
+
+  for (int q = tid; q < kTcInstr * 32; q += blockDim.x) sB[q] = Wt[q];
+  // generic-proxy stores, read below by the tensor core (async proxy)
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     su32(&tmem_base)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t4 = lane & 3;
-  uint32_t bw[kKSteps][2];
-#pragma unroll
-  for (int ks = 0; ks < kKSteps; ks++) {
-    bw[ks][0] = Wp[(ks * 32 + lane) * 2];
-    bw[ks][1] = Wp[(ks * 32 + lane) * 2 + 1];
+  if (tid == 0) {
+    for (int i = 0; i < kTcRing; i++) mbar_init(su32(&bar_full[i]), 1);
+    mbar_init(su32(&bar_mma[0]), 1);
+    mbar_init(su32(&bar_mma[1]), 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
+  tc_fence_before();
   __syncthreads();
-  const uint32_t* hw = reinterpret_cast<const uint32_t*>(halo);
-  for (int tl = warp; tl < (kBI / 16) * kBJ * kBK; tl += blockDim.x >> 5) {
-    const int ib = tl % (kBI / 16), jl = (tl / (kBI / 16)) % kBJ, kl = tl / ((kBI / 16) * kBJ);
-    const int j = bj0 + jl, k = bk0 + kl;
-    if (j >= a.Y || k >= a.Z) continue;  // warp-uniform
-    const int iA = bi0 + 16 * ib + g, iB = iA + 8;
-    // halo word of the slot at local i offset li, shifted by tap t
-    auto ld = [&](int li, int t) -> uint32_t {
-      const int hi = li + 1 + tap_di(t), hj = jl + 1 + tap_dj(t), hk = kl + 1 + tap_dk(t);
-      return hw[((hk * kHJ + hj) * kHI + hi) * 4 + t4];
-    };
-    const int liA = 16 * ib + g, liB = liA + 8;
-    float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
-#pragma unroll
-    for (int ks = 0; ks < kKSteps; ks++) {
-      const int t0 = 2 * ks, t1 = 2 * ks + 1;
-      const uint32_t a0 = ld(liA, t0);
-      const uint32_t a1 = ld(liB, t0);
-      uint32_t a2 = 0u, a3 = 0u;
-      if (t1 < kTaps) {
-        a2 = ld(liA, t1);
-        a3 = ld(liB, t1);
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+
+  // plane p -> ring slot and the parity of its use of that slot; plane k's
+  // accumulator (16 columns) and barrier alternate with k
+  auto slot = [&](int p) { return (p - k0 + 1) % kTcRing; };
+  auto parity = [&](int p) { return (uint32_t)(((p - k0 + 1) / kTcRing) & 1); };
+  auto acc = [&](int k) { return (k - k0) & 1; };
+  auto acc_parity = [&](int k) { return (uint32_t)(((k - k0) >> 1) & 1); };
+  // producer's bookkeeping (thread 0): windows issued / seen complete, and
+  // the last plane whose MMAs were committed
+  int issued = k0 - 2, waited = k0 - 2, committed = k0 - 1;
+  int seen = k0 - 1;  // the last plane whose MMA completion this thread saw
+  auto load = [&](int p) {
+    const uint32_t bar = su32(&bar_full[slot(p)]);
+    mbar_expect_tx(bar, (uint32_t)a.W * 16u);
+    bulk_load(su32(ring + slot(p) * a.wbytes),
+              inb + (long)p * a.XY + 128L * col - a.X - 1, (uint32_t)a.W * 16u, bar);
+    issued = p;
+  };
+  if (tid == 0) {
+    load(k0 - 1);
+    load(k0);
+    load(k0 + 1);
+  }
+  const uint32_t ring0 = su32(ring), sB0 = su32(sB);
+  // iteration k: the MMAs of plane k are issued, then the epilogue of plane
+  // k-1 runs while they execute.  The window loaded here (plane k+2) goes to
+  // the slot of plane k-3, whose last reader (the MMAs of plane k-2)
+  // completed before the previous epilogue.
+  for (int k = k0; k <= k1; k++) {
+    if (tid == 0 && k < k1) {
+      if (k + 2 <= k1) load(k + 2);
+      bool ok = true;
+      for (int p = waited + 1; p <= k + 1 && ok; p++) {
+        ok = mbar_wait(su32(&bar_full[slot(p)]), parity(p));
+        if (ok) waited = p;
       }
-      asm volatile(
-          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-          "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-          : "+f"(c0), "+f"(c1), "+f"(c2), "+f"(c3)
-          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(bw[ks][0]), "r"(bw[ks][1]));
-    }
-    // c0, c1: slot iA, channels 2*t4, 2*t4+1 ; c2, c3: slot iB
-    if (MODE == 0) {
-      uint32_t* hb = hid + (long)b * a.S * 4;
-      if (iA < a.X) hb[(((long)k * a.Y + j) * a.X + iA) * 4 + t4] = pack_bf16x2(c0, c1);
-      if (iB < a.X) hb[(((long)k * a.Y + j) * a.X + iB) * 4 + t4] = pack_bf16x2(c2, c3);
-    } else if (t4 < 3) {
-      const int comp = t4;
-      float2* ob = out + ((long)b * 3 + comp) * a.S;
-      auto put = [&](int i, float x, float y) {
-        if (i >= a.X) return;
-        const long s = ((long)k * a.Y + j) * a.X + i;
-        const bool unk = unknown_any(comp, a.n, i, j, k);
-        if (MODE == 1) {
-          if (unk) {
-            float2 v = ob[s];
-            v.x += x;
-            v.y += y;
-            ob[s] = v;
-          }
-        } else {
-          ob[s] = unk ? make_float2(x, y) : make_float2(0.f, 0.f);
+      if (ok) {
+        tc_fence_after();
+        const uint32_t d = tmem + 16u * (uint32_t)acc(k);
+#pragma unroll
+        for (int q = 0; q < kTcInstr; q++) {
+          const int dk = q / 5 - 1, pi = q % 5;
+          const int r0 = 2 * pi;
+          const int off0 = (r0 / 3 - 1) * a.X + (r0 % 3 - 1);
+          const int off1 = pi < 4 ? ((r0 + 1) / 3 - 1) * a.X + ((r0 + 1) % 3 - 1) : off0 + 1;
+          const uint32_t base = ring0 + slot(k + dk) * a.wbytes;
+          const uint64_t ad =
+              smem_desc(base + 16u * (uint32_t)(a.X + 1 + off0), 16u * (uint32_t)(off1 - off0), 128u);
+          const uint64_t bd = smem_desc(sB0 + 512u * q, 256u, 128u);
+          tc_mma(d, ad, bd, q > 0 ? 1u : 0u);
         }
-      };
-      put(iA, c0, c1);
-      put(iB, c2, c3);
+        tc_commit(su32(&bar_mma[acc(k)]));
+        committed = k;
+      } else {
+        failed = 1;
+        atomicExch(err, 1);
+      }
+    }
+    if (k > k0) {
+      const int ke = k - 1;  // plane of this epilogue
+      if (mbar_wait(su32(&bar_mma[acc(ke)]), acc_parity(ke))) {
+        seen = ke;
+      } else {
+        failed = 1;
+        atomicExch(err, 2);
+      }
+    }
+    __syncthreads();
+    if (failed) break;
+    if (k > k0) {
+      const int ke = k - 1;
+      tc_fence_after();
+      __syncwarp();
+      float v[8];
+      tc_load8(tmem + 16u * (uint32_t)acc(ke) + ((uint32_t)(warp * 32) << 16), v);
+      const int p = 128 * col + tid;
+      if (p < a.XY) {
+        const int j = p / a.X, i = p - j * a.X;
+        const long s = (long)ke * a.XY + p;
+        if (MODE == 0) {
+          uint4 h = make_uint4(0u, 0u, 0u, 0u);
+          if (i < a.X - 1 && j < a.Y - 1)
+            h = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]),
+                           pack_bf16x2(v[4], v[5]), pack_bf16x2(v[6], v[7]));
+          hid[(long)b * a.S + s] = h;
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            float2* ob = out + ((long)b * 3 + c) * a.S + s;
+            const bool unk = unknown_any(c, a.n, i, j, ke);
+            if (MODE == 1) {
+              if (unk) {
+                float2 w = *ob;
+                w.x += v[2 * c];
+                w.y += v[2 * c + 1];
+                *ob = w;
+              }
+            } else {
+              *ob = unk ? make_float2(v[2 * c], v[2 * c + 1]) : make_float2(0.f, 0.f);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+    }
+    __syncthreads();
+  }
+  // the last plane (no unknown edges): zeros for the hidden layer and c
+  if (MODE != 1 && !failed && chunk == a.nchunk - 1) {
+    const int p = 128 * col + tid;
+    if (p < a.XY) {
+      const long s = (long)(a.Z - 1) * a.XY + p;
+      if (MODE == 0) {
+        hid[(long)b * a.S + s] = make_uint4(0u, 0u, 0u, 0u);
+      } else {
+        for (int c = 0; c < 3; c++) out[((long)b * 3 + c) * a.S + s] = make_float2(0.f, 0.f);
+      }
     }
   }
+  if (tid == 0 && failed) {
+    // copies and MMAs still in flight finish before the shared and tensor
+    // memory are released
+    for (int p = waited + 1; p <= issued; p++) mbar_wait(su32(&bar_full[slot(p)]), parity(p));
+    for (int p = seen + 1; p <= committed; p++) mbar_wait(su32(&bar_mma[acc(p)]), acc_parity(p));
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  __syncwarp();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "r"(kTcCols)
+                 : "memory");
 }
 
 // ---------------------------------------------------------------- training
@@ -356,6 +559,9 @@ __global__ void __launch_bounds__(256) k_ls_dgrad(ConvArgs a, const float4* __re
       acc[ci] += sum;
     }
   }
+  // the hidden layer is zero on the last plane of each direction
+  if (i == a.X - 1 || j == a.Y - 1 || k == a.Z - 1)
+    for (int ci = 0; ci < kCh; ci++) acc[ci] = 0.f;
   gh[((long)b * a.S + s) * 2] = make_float4(acc[0], acc[1], acc[2], acc[3]);
   gh[((long)b * a.S + s) * 2 + 1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
 }
@@ -374,40 +580,85 @@ __global__ void k_ls_adam(float* __restrict__ W, const float* __restrict__ dW,
   W[i] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
 }
 
-ConvArgs conv_args(const int n[3], int nb, const int* mask) {
+ConvArgs conv_args(const int n[3], const int* mask) {
   ConvArgs a;
   for (int e = 0; e < 3; e++) a.n[e] = n[e];
   a.X = n[0] + 1;
   a.Y = n[1] + 1;
   a.Z = n[2] + 1;
   a.S = (long)a.X * a.Y * a.Z;
-  a.tiles = ((a.X + kBI - 1) / kBI) * ((a.Y + kBJ - 1) / kBJ) * ((a.Z + kBK - 1) / kBK);
+  a.XY = a.X * a.Y;
+  a.ncol = (a.XY + 127) / 128;
+  a.nchunk = (a.Z - 1 + kTcPlanes - 1) / kTcPlanes;
+  a.W = 128 + 2 * a.X + 3;
+  a.wbytes = (16 * a.W + 127) / 128 * 128;
   a.mask = mask;
-  (void)nb;
   return a;
 }
 
-unsigned conv_blocks(const ConvArgs& a) { return (unsigned)a.tiles; }
+// a waiting tensor-core convolution that gave up records why here (1: a
+// window copy, 2: the MMAs); read and cleared by learned_check
+__device__ int g_ls_err = 0;
+
+int* conv_err() {
+  static int* p = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaGetSymbolAddress((void**)&p, g_ls_err);
+    const int lim = kConvSmemMax;
+    cudaFuncSetAttribute(k_ls_conv<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_ls_conv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_ls_conv<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  });
+  return p;
+}
+
+template <int MODE>
+void launch_conv(const ConvArgs& a, int nb, const uint32_t* in, const uint4* Wt, uint32_t* hid,
+                 float2* out, cudaStream_t st) {
+  int* err = conv_err();
+  dim3 g((unsigned)(a.ncol * a.nchunk), nb);
+  k_ls_conv<MODE><<<g, 128, conv_smem(a), st>>>(a, reinterpret_cast<const uint4*>(in), Wt,
+                                                reinterpret_cast<uint4*>(hid), out, err);
+}
 
 }  // namespace
 
 // ---------------------------------------------------------------- host API
-void learned_pack(const float* dW32, uint32_t* dWp, cudaStream_t st) {
-  k_ls_pack<<<(2 * kKSteps * 32 + 127) / 128, 128, 0, st>>>(dW32, dWp);
+void learned_pack(const float* dW32, uint4* dWt, cudaStream_t st) {
+  k_ls_pack<<<(2 * kTcInstr * 32 + 127) / 128, 128, 0, st>>>(dW32, dWt);
 }
 
 // u += N(D^-1 (f - A u)) on the RHS that mask selects (level-0 view L)
-void learned_apply(const LevelView<float>& L, const uint32_t* Wp, uint32_t* X, uint32_t* H,
+void learned_apply(const LevelView<float>& L, const uint4* Wt, uint32_t* X, uint32_t* H,
                    cudaStream_t st) {
   dim3 g1((unsigned)((L.S + 255) / 256), L.nrhs);
   k_ls_input<<<g1, 256, 0, st>>>(L, nullptr, X);
-  ConvArgs a = conv_args(L.n, L.nrhs, L.active);
-  dim3 g2(conv_blocks(a), L.nrhs);
-  k_ls_conv<0><<<g2, 128, 0, st>>>(a, X, Wp, H, nullptr);
-  k_ls_conv<1><<<g2, 128, 0, st>>>(a, H, Wp + kKSteps * 32 * 2, nullptr, L.u);
+  ConvArgs a = conv_args(L.n, L.active);
+  launch_conv<0>(a, L.nrhs, X, Wt, H, nullptr, st);
+  launch_conv<1>(a, L.nrhs, H, Wt + kTcInstr * 32, nullptr, L.u, st);
 }
 
-size_t learned_scratch_bytes(long S, int nrhs) { return (size_t)2 * S * nrhs * 16; }
+// slots of zero guard before and after a bf16 slot buffer of the level
+long learned_guard(const int n[3]) { return kTcGuard(n[0] + 1, n[1] + 1); }
+
+// the shared memory one convolution needs on a level of n cells, or -1 if
+// it is more than a CTA can have
+long learned_smem(const int n[3]) {
+  const ConvArgs a = conv_args(n, nullptr);
+  const size_t b = conv_smem(a);
+  return b <= (size_t)kConvSmemMax ? (long)b : -1;
+}
+
+// a convolution's give-up code since the last check (0: none); clears it
+int learned_check(cudaStream_t st) {
+  int v = 0;
+  int* p = conv_err();
+  cudaMemcpyAsync(&v, p, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemsetAsync(p, 0, sizeof(int), st);
+  cudaStreamSynchronize(st);
+  return v;
+}
 
 // One training step over all samples (LevelView L: u = c buffer, f = r
 // samples, r = e buffer, nrhs = samples, op/wmu per sample).  Buffers:
@@ -415,7 +666,8 @@ size_t learned_scratch_bytes(long S, int nrhs) { return (size_t)2 * S * nrhs * 1
 // loss2 [B] (|e_b|^2 out), rn2 [B] (|r_b|^2 in); W [2][1728] fp32 master,
 // dW, m1, m2 same size, Wp packed.
 struct TrainBuffers {
-  uint32_t *X, *H, *Wp;
+  uint32_t *X, *H;  // guarded: learned_guard slots of zeros on both sides
+  uint4* Wt;
   float2 *c, *e, *t;
   float4 *gc, *gh;
   double *loss2, *rn2;
@@ -425,15 +677,14 @@ struct TrainBuffers {
 int learned_train_step(const LevelView<float>& L, const TrainBuffers& B, int step, float lr,
                        cudaStream_t st) {
   const int nb = L.nrhs;
-  ConvArgs a = conv_args(L.n, nb, nullptr);
+  ConvArgs a = conv_args(L.n, nullptr);
   dim3 gs((unsigned)((L.S + 255) / 256), nb);
-  dim3 gc(conv_blocks(a), nb);
   LevelView<float> V = L;
   V.active = nullptr;
   // forward: X = D^-1 r, H = W1 * X, c = W2 * H (masked)
   k_ls_input<<<gs, 256, 0, st>>>(V, V.f, B.X);
-  k_ls_conv<0><<<gc, 128, 0, st>>>(a, B.X, B.Wp, B.H, nullptr);
-  k_ls_conv<2><<<gc, 128, 0, st>>>(a, B.H, B.Wp + kKSteps * 32 * 2, nullptr, B.c);
+  launch_conv<0>(a, nb, B.X, B.Wt, B.H, nullptr, st);
+  launch_conv<2>(a, nb, B.H, B.Wt + kTcInstr * 32, nullptr, B.c, st);
   // e = r - A c and |e|^2
   cudaMemsetAsync(B.loss2, 0, nb * sizeof(double), st);
   LevelView<float> R = V;
@@ -458,7 +709,7 @@ int learned_train_step(const LevelView<float>& L, const TrainBuffers& B, int ste
     const float c1 = 1.f - powf(b1, (float)(step + 1)), c2 = 1.f - powf(b2, (float)(step + 1));
     k_ls_adam<<<(2 * kWLayer + 255) / 256, 256, 0, st>>>(B.W, B.dW, B.m1, B.m2, 2 * kWLayer, lr,
                                                         b1, b2, c1, c2, 1e-8f);
-    learned_pack(B.W, B.Wp, st);
+    learned_pack(B.W, B.Wt, st);
   }
   return cudaGetLastError() == cudaSuccess ? EMMI_OK : EMMI_ECUDA;
 }
@@ -484,7 +735,7 @@ int learned_after_cycle(emmi_solver* s, int h, const std::vector<int>& act) {
   }
   LevelView<float> L = s->view<float>(h, 0);
   L.active = s->d_learn;
-  learned_apply(L, s->d_lsWp, s->d_lsX, s->d_lsH, s->st);
+  learned_apply(L, s->d_lsWt, s->d_lsX, s->d_lsH, s->st);
   s->last_launches += 3;
   return EMMI_OK;
 }
@@ -595,8 +846,20 @@ int train_impl(emmi_solver* s, int steps, float lr, float* W, float* loss, float
   TrainAlloc A;
   TrainBuffers B;
   const size_t nw = 2 * kWLayer;
-  LCK(A.get(&B.X, (size_t)ns * S * 16));
-  LCK(A.get(&B.H, (size_t)ns * S * 16));
+  const int* nl0 = s->hier[0][0].n;
+  if (learned_smem(nl0) < 0) {
+    set_err("emmi_learned_train: rows of %d slots are wider than the convolution's shared-memory "
+            "window allows", nl0[0] + 1);
+    return EMMI_EINVAL;
+  }
+  const long gd = learned_guard(nl0);
+  const size_t xb = (size_t)(ns * S + 2 * gd) * 16;
+  LCK(A.get(&B.X, xb));
+  LCK(A.get(&B.H, xb));
+  LCK(cudaMemsetAsync(B.X, 0, xb, st));
+  LCK(cudaMemsetAsync(B.H, 0, xb, st));
+  B.X += 4 * gd;
+  B.H += 4 * gd;
   LCK(A.get(&B.c, (size_t)ns * 3 * S * sizeof(float2)));
   LCK(A.get(&B.e, (size_t)ns * 3 * S * sizeof(float2)));
   LCK(A.get(&B.t, (size_t)ns * 3 * S * sizeof(float2)));
@@ -608,11 +871,11 @@ int train_impl(emmi_solver* s, int steps, float lr, float* W, float* loss, float
   LCK(A.get(&B.dW, nw * sizeof(float)));
   LCK(A.get(&B.m1, nw * sizeof(float)));
   LCK(A.get(&B.m2, nw * sizeof(float)));
-  LCK(A.get(&B.Wp, (size_t)2 * kKSteps * 32 * 2 * sizeof(uint32_t)));
+  LCK(A.get(&B.Wt, (size_t)2 * kTcInstr * 32 * sizeof(uint4)));
   LCK(cudaMemcpyAsync(B.W, W, nw * sizeof(float), cudaMemcpyHostToDevice, st));
   LCK(cudaMemsetAsync(B.m1, 0, nw * sizeof(float), st));
   LCK(cudaMemsetAsync(B.m2, 0, nw * sizeof(float), st));
-  learned_pack(B.W, B.Wp, st);
+  learned_pack(B.W, B.Wt, st);
   std::vector<double> rn2(ns), l2(ns);
   LCK(cudaMemcpyAsync(rn2.data(), s->d_srn2, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
   LevelView<float> L = sample_view(s);
@@ -629,6 +892,10 @@ int train_impl(emmi_solver* s, int steps, float lr, float* W, float* loss, float
     double sum = 0;
     for (int k = 0; k < ns; k++) sum += rn2[k] > 0 ? l2[k] / rn2[k] : 0.0;
     if (loss) loss[it] = (float)(sum / ns);
+  }
+  if (const int why = learned_check(st)) {
+    set_err("emmi_learned_train: a tensor-core convolution gave up waiting (code %d)", why);
+    return EMMI_ECUDA;
   }
   if (grad) {
     LCK(cudaMemcpyAsync(grad, B.dW, nw * sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -711,6 +978,24 @@ int emmi_learned_add_samples(emmi_solver* s, int ns, const float* r, const int* 
 
 int emmi_learned_samples(const emmi_solver* s) { return s ? s->ls_count : 0; }
 
+int emmi_learned_apply(emmi_solver* s, const void* f, void* u) {
+  if (!s || !f || !u || !s->learned_on) {
+    set_err("emmi_learned_apply: bad argument (a solver with weights set, f and u)");
+    return EMMI_EINVAL;
+  }
+  LevelView<float> L = s->view<float>(0, 0);
+  L.f = reinterpret_cast<float2*>(const_cast<void*>(f));
+  L.u = reinterpret_cast<float2*>(u);
+  L.active = nullptr;
+  learned_apply(L, s->d_lsWt, s->d_lsX, s->d_lsH, s->st);
+  LCK(cudaGetLastError());
+  if (const int why = learned_check(s->st)) {
+    set_err("emmi_learned_apply: a tensor-core convolution gave up waiting (code %d)", why);
+    return EMMI_ECUDA;
+  }
+  return EMMI_OK;
+}
+
 int emmi_learned_train(emmi_solver* s, int steps, float lr, float* W, float* loss) {
   return train_impl(s, steps, lr, W, loss, nullptr);
 }
@@ -734,18 +1019,31 @@ int emmi_learned_set(emmi_solver* s, const float* W) {
     return EMMI_OK;
   }
   const long S = s->hier[0][0].S;
+  const int* nl0 = s->hier[0][0].n;
+  if (learned_smem(nl0) < 0) {
+    set_err("emmi_learned_set: rows of %d slots are wider than the convolution's shared-memory "
+            "window allows", nl0[0] + 1);
+    return EMMI_EINVAL;
+  }
   int rc;
   if (!s->d_lsW) {
+    // X and H: [nrhs][S] bf16 slots between two zero guards
+    const long gd = learned_guard(nl0);
+    const size_t xb = (size_t)(s->nrhs * S + 2 * gd) * 16;
+    uint32_t *rx = nullptr, *rh = nullptr;
     if ((rc = s->alloc((void**)&s->d_lsW, 2 * kWLayer * sizeof(float))) != EMMI_OK) return rc;
-    if ((rc = s->alloc((void**)&s->d_lsWp, (size_t)2 * kKSteps * 32 * 2 * sizeof(uint32_t))) !=
-        EMMI_OK)
+    if ((rc = s->alloc((void**)&s->d_lsWt, (size_t)2 * kTcInstr * 32 * sizeof(uint4))) != EMMI_OK)
       return rc;
-    if ((rc = s->alloc((void**)&s->d_lsX, (size_t)s->nrhs * S * 16)) != EMMI_OK) return rc;
-    if ((rc = s->alloc((void**)&s->d_lsH, (size_t)s->nrhs * S * 16)) != EMMI_OK) return rc;
+    if ((rc = s->alloc((void**)&rx, xb)) != EMMI_OK) return rc;
+    if ((rc = s->alloc((void**)&rh, xb)) != EMMI_OK) return rc;
     if ((rc = s->alloc((void**)&s->d_learn, (size_t)s->nrhs * sizeof(int))) != EMMI_OK) return rc;
+    LCK(cudaMemsetAsync(rx, 0, xb, s->st));
+    LCK(cudaMemsetAsync(rh, 0, xb, s->st));
+    s->d_lsX = rx + 4 * gd;
+    s->d_lsH = rh + 4 * gd;
   }
   LCK(cudaMemcpyAsync(s->d_lsW, W, 2 * kWLayer * sizeof(float), cudaMemcpyHostToDevice, s->st));
-  learned_pack(s->d_lsW, s->d_lsWp, s->st);
+  learned_pack(s->d_lsW, s->d_lsWt, s->st);
   LCK(cudaStreamSynchronize(s->st));
   s->learned_on = true;
   return EMMI_OK;

@@ -1072,6 +1072,13 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
                       : std::isfinite(rn[r]) ? EMMI_SOLVE_MAXIT : EMMI_SOLVE_NONFINITE;
         }
     }
+    if (s->learned_on) {
+      if (const int why = learned_check(s->st)) {
+        set_err("emmi_solver_solve: a learned-correction convolution gave up waiting (code %d)",
+                why);
+        return EMMI_ECUDA;
+      }
+    }
   } else {
     // plain FP64 cycles on u64/f64 (gmg_apply, gmg.c:1911-1926)
     for (int icycle = 0; icycle < ncycle; icycle++) {

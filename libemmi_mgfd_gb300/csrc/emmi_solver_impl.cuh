@@ -100,12 +100,13 @@ struct emmi_solver {
   double* d_kscale = nullptr;
   int* d_kj = nullptr;
 
-  // learned correction after each complex64 cycle (level 0): fp32 master and
-  // packed bf16 weights, bf16 input/hidden planes [nrhs][S][8], per-RHS
-  // enable mask (cleared for a RHS that falls back to plain cycles)
+  // learned correction after each complex64 cycle (level 0): fp32 master
+  // weights and their tensor-core B operands, bf16 input/hidden slots
+  // [nrhs][S][8] between zero guards, per-RHS enable mask (cleared for a RHS
+  // that falls back to plain cycles)
   bool learned_on = false;
   float* d_lsW = nullptr;
-  uint32_t* d_lsWp = nullptr;
+  uint4* d_lsWt = nullptr;
   uint32_t *d_lsX = nullptr, *d_lsH = nullptr;
   int* d_learn = nullptr;
   std::vector<int> h_learn, h_fallback;
@@ -157,4 +158,7 @@ int learned_snapshot(emmi_solver* s, int h, const std::vector<int>& act);
 // a RHS that stalls with the learned correction drops back to plain cycles;
 // returns true when it did
 bool learned_fallback(emmi_solver* s, int r);
+// nonzero when a learned-correction convolution gave up waiting since the
+// last call (synchronises the stream; clears the record)
+int learned_check(cudaStream_t st);
 }  // namespace emmi

@@ -284,6 +284,16 @@ class Solver:
         W = np.ascontiguousarray(W, np.float32)
         _check(lib().emmi_learned_set(self._h, _p(W)), "emmi_learned_set")
 
+    def learned_apply(self, f, u):
+        """One application of the weights set by set_learned, in place:
+        u += N(D^-1 (f - A u)); f, u torch complex64 tensors [nrhs, 3S] on
+        the GPU."""
+        import torch
+        torch.cuda.synchronize()
+        _check(lib().emmi_learned_apply(self._h, C.c_void_p(f.data_ptr()),
+                                        C.c_void_p(u.data_ptr())), "emmi_learned_apply")
+        torch.cuda.synchronize()
+
     @property
     def last_time(self) -> float:
         return lib().emmi_solver_last_time(self._h)

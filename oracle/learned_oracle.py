@@ -10,7 +10,9 @@ network's definition:
 
   z      = D^-1 r on unknown edges (D the diagonal of A), 8 channels per slot
            (Ex, Ey, Ez real/imaginary, 2 zero channels), bf16-rounded
-  h      = conv(z, W1) rounded to bf16      (3x3x3, zero padding)
+  h      = conv(z, W1) rounded to bf16      (3x3x3, zero padding), set to
+           zero on the last slot plane of each direction (i = n1, j = n2,
+           k = n3: no component has an unknown edge there)
   c      = conv(h, W2), channels 0..5 -> complex components, unknown edges
   loss_b = |r_b - A c_b|^2 / |r_b|^2
 
@@ -49,6 +51,15 @@ def unknown_masks(n):
         p, q = (c + 1) % 3, (c + 2) % 3
         out.append((P[c] < n[c]) & (P[p] >= 1) & (P[p] < n[p]) & (P[q] >= 1) & (P[q] < n[q]))
     return np.stack(out)
+
+
+def far_mask(shape):
+    """[Z, Y, X] 1.0 off the last plane of each direction, 0.0 on it."""
+    m = np.ones(shape)
+    m[-1, :, :] = 0.0
+    m[:, -1, :] = 0.0
+    m[:, :, -1] = 0.0
+    return m
 
 
 def diagonal(level):
@@ -115,6 +126,7 @@ class Net:
         self.S = int(np.prod(self.shape))
         self.mask = unknown_masks(level.n)
         self.diag = diagonal(level).reshape(3, *self.shape)
+        self.far = far_mask(self.shape)[..., None]
         self.rb = bf16_round
 
     def _round(self, a):
@@ -132,7 +144,7 @@ class Net:
     def forward(self, W, r):
         w = self._round(np.asarray(W, np.float64).reshape(2, TAPS, CH, CH))
         x = self.channels(r)
-        h = self._round(conv(x, w[0]))
+        h = self._round(conv(x, w[0])) * self.far
         o = conv(h, w[1])
         c = np.zeros((3, *self.shape), np.complex128)
         for k in range(3):
@@ -157,7 +169,7 @@ class Net:
                 gc[..., 2 * k] = np.where(self.mask[k], -2.0 * q[k].real / rn2, 0.0)
                 gc[..., 2 * k + 1] = np.where(self.mask[k], 2.0 * q[k].imag / rn2, 0.0)
             grad[1] += weight_grad(gc, h)
-            gh = conv_transpose(gc, w[1])
+            gh = conv_transpose(gc, w[1]) * self.far
             grad[0] += weight_grad(gh, x)
         return total / len(samples), grad.reshape(-1)
 

@@ -45,6 +45,46 @@ def test_gpu_loss_and_gradient_match_oracle(golden):
 
 
 @gpu
+def test_gpu_correction_matches_oracle(golden):
+    """One deployment application (residual, two tensor-core convolutions,
+    u += c on unknown edges) on two RHS of one batch against the oracle's
+    network: the second RHS's convolution windows start in the first RHS's
+    last plane, the first RHS's in the buffer's zero guard."""
+    import torch
+    from libemmi_mgfd_gb300 import gpu as G
+    from learned_oracle import unknown_masks
+    g = golden("tiny_layered")
+    n, x, raw, om = golden_level(g)
+    oms = np.array([om, 0.5 * om], np.float32)
+    s = G.Solver(n, *[v.astype(np.float32) for v in x], raw[None], oms, op=np.zeros(2, np.int32),
+                 options=G.Options(precision=G.PREC_MIXED, sigma_floor=1e-30))
+    xs = [v.astype(np.float32).astype(np.float64) for v in x]
+    c = weighted_cells(n, xs, raw)
+    rng = np.random.default_rng(7)
+    W = (0.05 * rng.standard_normal((2, TAPS, CH, CH))).astype(np.float32).reshape(-1)
+    s.set_learned(W)
+    unk = unknown_masks(n).reshape(-1)
+    S3 = unk.size
+    u = np.zeros((2, S3), np.complex64)
+    f = np.zeros((2, S3), np.complex64)
+    for r in range(2):
+        u[r][unk] = rng.standard_normal(unk.sum()) + 1j * rng.standard_normal(unk.sum())
+        f[r][unk] = rng.standard_normal(unk.sum()) + 1j * rng.standard_normal(unk.sum())
+    du = torch.tensor(u, device="cuda")
+    df = torch.tensor(f, device="cuda")
+    s.learned_apply(df, du)
+    got = du.cpu().numpy().astype(np.complex128) - u.astype(np.complex128)
+    for r in range(2):
+        lev = O.Level(n, xs, c[:3], c[3], float(oms[r]))
+        net = Net(lev, bf16_round=True)
+        res = f[r].astype(np.complex128) - lev.apply(u[r].astype(np.complex128))
+        want, _ = net.forward(W.astype(np.float64), res)
+        err = np.linalg.norm(got[r] - want) / np.linalg.norm(want)
+        assert err < 2e-3, (r, err)
+        assert np.all(got[r][~unk] == 0)
+
+
+@gpu
 def test_training_on_gpu_reduces_the_loss():
     from libemmi_mgfd_gb300 import learned as LS
     out = LS.train(n=32, models=3, per_rhs=4, steps=120, lr=3e-3, seed=200)

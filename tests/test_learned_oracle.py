@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from learned_oracle import Net, TAPS, CH, bf16, conv, conv_transpose
+from learned_oracle import Net, TAPS, CH, bf16, conv, conv_transpose, far_mask, taps
 from _cases import random_level
 
 
@@ -21,6 +21,33 @@ def test_conv_transpose_is_the_adjoint():
     g = rng.standard_normal((4, 5, 6, CH))
     w = rng.standard_normal((TAPS, CH, CH))
     assert np.isclose(np.sum(conv(x, w) * g), np.sum(x * conv_transpose(g, w)), rtol=1e-12)
+
+
+@pytest.mark.parametrize("shape", [(5, 6, 7), (3, 4, 17), (6, 3, 3)])
+def test_flattened_convolution_equals_zero_padded_off_the_last_planes(shape):
+    """The tensor-core kernels convolve on the flattened slot index
+    s = i + X j + X Y k, two right-hand sides back to back between zero
+    guards: a tap that leaves the grid lands on the last plane of a lower
+    direction, on the other RHS's last plane or in a guard.  With inputs zero
+    on the last plane of each direction (no unknown edge there; the hidden
+    layer is masked to zero there) this equals the zero-padded convolution
+    everywhere off those planes, the only slots whose outputs are used."""
+    rng = np.random.default_rng(2)
+    Z, Y, X = shape
+    m = far_mask(shape)[..., None]
+    xs = [rng.standard_normal((Z, Y, X, CH)) * m for _ in range(2)]
+    w = rng.standard_normal((TAPS, CH, CH))
+    S, G = Z * Y * X, X * Y + X + 1
+    flat = np.concatenate([np.zeros((G, CH))] + [x.reshape(-1, CH) for x in xs]
+                          + [np.zeros((G, CH))])
+    keep = m[..., 0].astype(bool)
+    for b in range(2):
+        out = np.zeros((S, CH))
+        for t, (di, dj, dk) in enumerate(taps()):
+            o = G + b * S + di + X * dj + X * Y * dk
+            out += flat[o:o + S] @ w[t]
+        ref = conv(xs[b], w)
+        assert np.allclose(out.reshape(Z, Y, X, CH)[keep], ref[keep], rtol=1e-12, atol=1e-12)
 
 
 def test_bf16_rounds_to_nearest_even():
