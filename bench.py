@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--profile", action="store_true",
                    help="one shot: a short solve, then one level-0 line sweep inside the NVTX "
                         "range emmi_profile (for ncu --nvtx-include emmi_profile/)")
+    p.add_argument("--profile-dir", type=int, default=0, choices=(0, 1, 2),
+                   help="with --profile: the line direction of the sweep (0 x, 1 y, 2 z)")
     p.add_argument("--profile-learned", action="store_true",
                    help="with --profile: one application of the learned correction (seeded "
                         "weights, seeded level-0 iterates) instead of the line sweep")
@@ -272,7 +274,7 @@ def main():
             torch.cuda.nvtx.range_pop()
         else:
             torch.cuda.nvtx.range_push("emmi_profile")
-            sp.time_smoother(0, reps=1)
+            sp.time_smoother(a.profile_dir, reps=1)
             torch.cuda.nvtx.range_pop()
         sp.close()
         print(json.dumps({"profile": "done", "n": a.n, "nrhs": nrhs}))

@@ -162,6 +162,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
                : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ uint32_t mbar_test(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -231,25 +234,27 @@ __device__ __forceinline__ void tc_load8(uint32_t taddr, float (&v)[8]) {
 
 // One 3x3x3 convolution, 8 -> 8 channels, bf16 slots [b][S] (16 bytes per
 // slot) with kTcGuard(X, Y) zero slots before the first and after the last
-// right-hand side.  A CTA of 4 warps owns one column of 128 consecutive
-// in-plane slots (p = i + X j in [128 col, 128 col + 128)) and walks the
-// planes k of one chunk; for plane k the output tile is D[m][n] =
-// sum_taps X[s_m + off(tap)] W_tap, 15 tcgen05.mma (M = 128 slots, N = 16,
-// K = 16) into one of two tensor-memory accumulators, so that the MMAs of
-// plane k run while the epilogue of plane k-1 reads the other one back.
-// Each plane's window (slots 128 col - X - 1 ... 128 col + 127 + X + 2 of
-// that plane, contiguous) comes in by one bulk copy, two planes ahead, into
-// a ring of 5 windows; the window serves as the A operand of the plane's
-// three dk roles directly: tap (di, dj) of a window is the 128-row matrix
-// starting X + 1 + X dj + di slots in (rows 16 bytes apart, 8 channels each
-// = one core-matrix row).
+// right-hand side.  A CTA owns one column of 128 consecutive in-plane slots
+// (p = i + X j) and walks the planes k of one chunk; the tile of plane k is
+// D[m][n] = sum_taps X[s_m + off(tap)] W_tap, 15 tcgen05.mma (M = 128 slots,
+// N = 16, K = 16) into one of two tensor-memory accumulators.  One thread of
+// the producer warp issues the copies and the MMAs; 4 epilogue warps (one
+// TMEM lane per thread) read the accumulators back and store; the two sides
+// meet only at mbarriers (window landed, accumulator ready, accumulator read
+// back), so the MMAs of the next planes run while an epilogue stores.  Each
+// plane's window (slots p0 - X - 1 ... p0 + 127 + X + 2 of that plane,
+// contiguous) comes in by one bulk copy, kTcAhead planes ahead, into a ring
+// of kTcRing windows; the window serves as the A operand of the plane's
+// three dk roles directly: tap (di, dj) is the 128-row matrix starting
+// X + 1 + X dj + di slots in (rows 16 bytes apart, 8 channels each = one
+// core-matrix row).
 //   MODE 0: hidden layer, bf16 [b][S] (guarded layout), zero on the planes
 //           i = X-1, j = Y-1, k = Z-1
 //   MODE 1: u += channels 0..5 on unknown edges (deployment)
 //   MODE 2: c = channels 0..5 on unknown edges, 0 elsewhere ([b][3][S])
 // Plane k = Z-1 holds no unknown edge: it is never computed (MODE 0 and 2
 // write its zeros).  Waits are bounded; a CTA that gives up sets *err,
-// drains its copies and frees its tensor memory.
+// drains its copies and MMAs and frees its tensor memory.
 struct ConvArgs {
   int n[3];      // cells of the level
   int X, Y, Z;   // slots per direction (n+1)
@@ -262,9 +267,12 @@ struct ConvArgs {
   const int* mask;
 };
 
-constexpr int kTcRing = 5;
-constexpr int kTcPlanes = 32;  // planes per chunk
-constexpr int kTcCols = 32;    // tensor-memory columns allocated (16 used)
+constexpr int kTcEpiWarps = 4;  // epilogue warps (TMEM lanes 0..127); one producer warp
+constexpr int kTcThreads = 32 * (kTcEpiWarps + 1);
+constexpr int kTcRing = 7;      // plane windows in shared memory
+constexpr int kTcAhead = kTcRing - 3;  // planes loaded ahead of the MMAs
+constexpr int kTcPlanes = 32;   // planes per chunk
+constexpr int kTcCols = 32;     // tensor memory: 2 accumulators x 16 columns
 // dynamic shared memory a CTA may ask for (227 KB less the static part)
 constexpr int kConvSmemMax = 227 * 1024 - 1024;
 __host__ __device__ inline long kTcGuard(int X, int Y) { return (long)X * Y + X + 129; }
@@ -273,15 +281,17 @@ inline size_t conv_smem(const ConvArgs& a) {
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __restrict__ in,
-                                                 const uint4* __restrict__ Wt,
-                                                 uint4* __restrict__ hid,
-                                                 float2* __restrict__ out, int* __restrict__ err) {
+__global__ void __launch_bounds__(kTcThreads) k_ls_conv(ConvArgs a, const uint4* __restrict__ in,
+                                                        const uint4* __restrict__ Wt,
+                                                        uint4* __restrict__ hid,
+                                                        float2* __restrict__ out,
+                                                        int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char dsm[];
-  __shared__ __align__(8) uint64_t bar_full[kTcRing];
-  __shared__ __align__(8) uint64_t bar_mma[2];
+  __shared__ __align__(8) uint64_t bar_full[kTcRing];  // window landed (bulk copy)
+  __shared__ __align__(8) uint64_t bar_done[2];        // accumulator ready (tcgen05.commit)
+  __shared__ __align__(8) uint64_t bar_free[2];        // accumulator read back (4 epilogue warps)
   __shared__ uint32_t tmem_base;
-  __shared__ int failed;
+  __shared__ volatile int failed;
   const int b = blockIdx.y;
   if (a.mask && !a.mask[b]) return;
   if (*(volatile int*)err) return;  // an earlier CTA gave up: the launch has failed
@@ -291,7 +301,7 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
   const int tid = threadIdx.x, warp = tid >> 5;
   uint4* sB = reinterpret_cast<uint4*>(dsm);
   unsigned char* ring = dsm + kTcInstr * 512;
-  const uint4* inb = in + (long)b * a.S;
+  const int p0 = 128 * col;  // first in-plane slot of the column
 
   for (int q = tid; q < kTcInstr * 32; q += blockDim.x) sB[q] = Wt[q];
   // generic-proxy stores, read below by the tensor core (async proxy)
@@ -306,8 +316,10 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
   }
   if (tid == 0) {
     for (int i = 0; i < kTcRing; i++) mbar_init(su32(&bar_full[i]), 1);
-    mbar_init(su32(&bar_mma[0]), 1);
-    mbar_init(su32(&bar_mma[1]), 1);
+    for (int i = 0; i < 2; i++) {
+      mbar_init(su32(&bar_done[i]), 1);
+      mbar_init(su32(&bar_free[i]), 4);
+    }
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -317,41 +329,41 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
   const uint32_t tmem = tmem_base;
 
   // plane p -> ring slot and the parity of its use of that slot; plane k's
-  // accumulator (16 columns) and barrier alternate with k
+  // accumulator (16 columns) alternates with k, its u-th use has parity u & 1
   auto slot = [&](int p) { return (p - k0 + 1) % kTcRing; };
   auto parity = [&](int p) { return (uint32_t)(((p - k0 + 1) / kTcRing) & 1); };
   auto acc = [&](int k) { return (k - k0) & 1; };
-  auto acc_parity = [&](int k) { return (uint32_t)(((k - k0) >> 1) & 1); };
-  // producer's bookkeeping (thread 0): windows issued / seen complete, and
-  // the last plane whose MMAs were committed
-  int issued = k0 - 2, waited = k0 - 2, committed = k0 - 1;
-  int seen = k0 - 1;  // the last plane whose MMA completion this thread saw
-  auto load = [&](int p) {
-    const uint32_t bar = su32(&bar_full[slot(p)]);
-    mbar_expect_tx(bar, (uint32_t)a.W * 16u);
-    bulk_load(su32(ring + slot(p) * a.wbytes),
-              inb + (long)p * a.XY + 128L * col - a.X - 1, (uint32_t)a.W * 16u, bar);
-    issued = p;
-  };
-  if (tid == 0) {
-    load(k0 - 1);
-    load(k0);
-    load(k0 + 1);
-  }
-  const uint32_t ring0 = su32(ring), sB0 = su32(sB);
-  // iteration k: the MMAs of plane k are issued, then the epilogue of plane
-  // k-1 runs while they execute.  The window loaded here (plane k+2) goes to
-  // the slot of plane k-3, whose last reader (the MMAs of plane k-2)
-  // completed before the previous epilogue.
-  for (int k = k0; k <= k1; k++) {
-    if (tid == 0 && k < k1) {
-      if (k + 2 <= k1) load(k + 2);
-      bool ok = true;
-      for (int p = waited + 1; p <= k + 1 && ok; p++) {
-        ok = mbar_wait(su32(&bar_full[slot(p)]), parity(p));
-        if (ok) waited = p;
-      }
-      if (ok) {
+  auto use = [&](int k) { return (uint32_t)(((k - k0) >> 1) & 1); };
+
+  if (warp == kTcEpiWarps) {
+    // ---- producer: one thread issues the window copies and the MMAs
+    if ((tid & 31) == 0) {
+      const uint4* inb = in + (long)b * a.S;
+      int issued = k0 - 2, waited = k0 - 2, committed = k0 - 1;
+      auto load = [&](int p) {
+        const uint32_t bar = su32(&bar_full[slot(p)]);
+        mbar_expect_tx(bar, (uint32_t)a.W * 16u);
+        bulk_load(su32(ring + slot(p) * a.wbytes), inb + (long)p * a.XY + p0 - a.X - 1,
+                  (uint32_t)a.W * 16u, bar);
+        issued = p;
+      };
+      for (int p = k0 - 1; p <= min(k0 + kTcAhead - 1, k1); p++) load(p);
+      const uint32_t ring0 = su32(ring), sB0 = su32(sB);
+      for (int k = k0; k < k1; k++) {
+        bool ok = true;
+        // accumulator acc(k) and the window slot of plane k-3 are free once
+        // the epilogue of plane k-2 has read its accumulator back
+        if (k - 2 >= k0) ok = mbar_wait(su32(&bar_free[acc(k)]), use(k) ^ 1u);
+        if (ok && k + kTcAhead <= k1) load(k + kTcAhead);
+        for (int p = waited + 1; p <= k + 1 && ok; p++) {
+          ok = mbar_wait(su32(&bar_full[slot(p)]), parity(p));
+          if (ok) waited = p;
+        }
+        if (!ok || failed) {
+          failed = 1;
+          atomicExch(err, 1);
+          break;
+        }
         tc_fence_after();
         const uint32_t d = tmem + 16u * (uint32_t)acc(k);
 #pragma unroll
@@ -361,39 +373,44 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
           const int off0 = (r0 / 3 - 1) * a.X + (r0 % 3 - 1);
           const int off1 = pi < 4 ? ((r0 + 1) / 3 - 1) * a.X + ((r0 + 1) % 3 - 1) : off0 + 1;
           const uint32_t base = ring0 + slot(k + dk) * a.wbytes;
-          const uint64_t ad =
-              smem_desc(base + 16u * (uint32_t)(a.X + 1 + off0), 16u * (uint32_t)(off1 - off0), 128u);
+          const uint64_t ad = smem_desc(base + 16u * (uint32_t)(a.X + 1 + off0),
+                                        16u * (uint32_t)(off1 - off0), 128u);
           const uint64_t bd = smem_desc(sB0 + 512u * q, 256u, 128u);
           tc_mma(d, ad, bd, q > 0 ? 1u : 0u);
         }
-        tc_commit(su32(&bar_mma[acc(k)]));
+        tc_commit(su32(&bar_done[acc(k)]));
         committed = k;
-      } else {
-        failed = 1;
-        atomicExch(err, 1);
+      }
+      if (failed) {
+        // copies and MMAs in flight finish before shared and tensor memory go
+        for (int p = waited + 1; p <= issued; p++) mbar_wait(su32(&bar_full[slot(p)]), parity(p));
+        if (committed >= k0) mbar_wait(su32(&bar_done[acc(committed)]), use(committed));
       }
     }
-    if (k > k0) {
-      const int ke = k - 1;  // plane of this epilogue
-      if (mbar_wait(su32(&bar_mma[acc(ke)]), acc_parity(ke))) {
-        seen = ke;
-      } else {
-        failed = 1;
-        atomicExch(err, 2);
+  } else {
+    // ---- epilogue: 4 warps, thread tid reads TMEM lane tid (output slot p0 + tid)
+    const int p = p0 + tid;
+    const bool live = p < a.XY;
+    const int j = live ? p / a.X : 0, i = p - j * a.X;
+    for (int k = k0; k < k1; k++) {
+      const bool late = !mbar_wait(su32(&bar_done[acc(k)]), use(k));
+      // the warp leaves together (tcgen05.ld below is warp-collective)
+      if (__any_sync(0xffffffffu, late || failed)) {
+        if (late) {
+          failed = 1;
+          atomicExch(err, 2);
+        }
+        break;
       }
-    }
-    __syncthreads();
-    if (failed) break;
-    if (k > k0) {
-      const int ke = k - 1;
       tc_fence_after();
       __syncwarp();
       float v[8];
-      tc_load8(tmem + 16u * (uint32_t)acc(ke) + ((uint32_t)(warp * 32) << 16), v);
-      const int p = 128 * col + tid;
-      if (p < a.XY) {
-        const int j = p / a.X, i = p - j * a.X;
-        const long s = (long)ke * a.XY + p;
+      tc_load8(tmem + 16u * (uint32_t)acc(k) + ((uint32_t)(warp * 32) << 16), v);
+      tc_fence_before();
+      __syncwarp();
+      if ((tid & 31) == 0) mbar_arrive(su32(&bar_free[acc(k)]));
+      if (live) {
+        const long s = (long)k * a.XY + p;
         if (MODE == 0) {
           uint4 h = make_uint4(0u, 0u, 0u, 0u);
           if (i < a.X - 1 && j < a.Y - 1)
@@ -404,7 +421,7 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             float2* ob = out + ((long)b * 3 + c) * a.S + s;
-            const bool unk = unknown_any(c, a.n, i, j, ke);
+            const bool unk = unknown_any(c, a.n, i, j, k);
             if (MODE == 1) {
               if (unk) {
                 float2 w = *ob;
@@ -418,14 +435,9 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
           }
         }
       }
-      tc_fence_before();
     }
-    __syncthreads();
-  }
-  // the last plane (no unknown edges): zeros for the hidden layer and c
-  if (MODE != 1 && !failed && chunk == a.nchunk - 1) {
-    const int p = 128 * col + tid;
-    if (p < a.XY) {
+    // the last plane (no unknown edges): zeros for the hidden layer and c
+    if (MODE != 1 && !failed && chunk == a.nchunk - 1 && live) {
       const long s = (long)(a.Z - 1) * a.XY + p;
       if (MODE == 0) {
         hid[(long)b * a.S + s] = make_uint4(0u, 0u, 0u, 0u);
@@ -433,12 +445,6 @@ __global__ void __launch_bounds__(128) k_ls_conv(ConvArgs a, const uint4* __rest
         for (int c = 0; c < 3; c++) out[((long)b * 3 + c) * a.S + s] = make_float2(0.f, 0.f);
       }
     }
-  }
-  if (tid == 0 && failed) {
-    // copies and MMAs still in flight finish before the shared and tensor
-    // memory are released
-    for (int p = waited + 1; p <= issued; p++) mbar_wait(su32(&bar_full[slot(p)]), parity(p));
-    for (int p = seen + 1; p <= committed; p++) mbar_wait(su32(&bar_mma[acc(p)]), acc_parity(p));
   }
   tc_fence_before();
   __syncthreads();
@@ -618,7 +624,7 @@ void launch_conv(const ConvArgs& a, int nb, const uint32_t* in, const uint4* Wt,
                  float2* out, cudaStream_t st) {
   int* err = conv_err();
   dim3 g((unsigned)(a.ncol * a.nchunk), nb);
-  k_ls_conv<MODE><<<g, 128, conv_smem(a), st>>>(a, reinterpret_cast<const uint4*>(in), Wt,
+  k_ls_conv<MODE><<<g, kTcThreads, conv_smem(a), st>>>(a, reinterpret_cast<const uint4*>(in), Wt,
                                                 reinterpret_cast<uint4*>(hid), out, err);
 }
 
