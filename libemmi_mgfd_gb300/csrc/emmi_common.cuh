@@ -146,11 +146,12 @@ __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const 
                                           EdgeCoef<T>& e) {
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
   const int a = P[C], b = P[p], g = P[q];
-  const long cs[3] = {1, (long)n[0], (long)n[0] * n[1]};
-  const long c11 = a * cs[C] + (long)b * cs[p] + (long)g * cs[q];  // cell (p=b, q=g)
-  const long c10 = c11 - cs[q];                                     // (b, g-1)
-  const long c01 = c11 - cs[p];                                     // (b-1, g)
-  const long c00 = c01 - cs[q];                                     // (b-1, g-1)
+  // 32-bit cell offsets (a level has fewer than 2^31 cells)
+  const int cs[3] = {1, n[0], n[0] * n[1]};
+  const int c11 = a * cs[C] + b * cs[p] + g * cs[q];  // cell (p=b, q=g)
+  const int c10 = c11 - cs[q];                         // (b, g-1)
+  const int c01 = c11 - cs[p];                         // (b-1, g)
+  const int c00 = c01 - cs[q];                         // (b-1, g-1)
   const T s = T(0.25) * (((ldro(sigC + c00) + ldro(sigC + c01)) + ldro(sigC + c10)) + ldro(sigC + c11));
   const T i00 = ldro(imu + c00), i01 = ldro(imu + c01), i10 = ldro(imu + c10), i11 = ldro(imu + c11);
   const T m1 = T(0.5) * (i11 + i10);  // H_q face at p=b
@@ -181,12 +182,19 @@ __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const 
 }
 
 // slot offset of neighbour k of a component-C edge, in slot units, plus its
-// component's base offset (comp*S)
+// component's base offset (comp*S); 32-bit: a level's 3 S edge slots fit in
+// an int (emmi_solver_create refuses larger grids)
 template <int C>
 __device__ __forceinline__ long nbr_slot_delta(int k, const long ss[3], long S) {
   const NbrOff o = nbr_off(C, k);
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
   return (long)o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
+}
+template <int C>
+__device__ __forceinline__ int nbr_delta32(int k, const int ss[3], int S) {
+  const NbrOff o = nbr_off(C, k);
+  constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
+  return o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
 }
 
 // slot index -> node indices with 32-bit arithmetic (a level holds fewer
@@ -207,14 +215,17 @@ __device__ __forceinline__ C_t<T> apply_row(const LevelView<T>& L, const C_t<T>*
                                             const int P[3], long s, const long ss[3],
                                             EdgeCoef<T>& e) {
   // u, cells and geometry are not written by any thread while a residual,
-  // an assembly or a same-colour block sweep reads them: read-only loads
+  // an assembly or a same-colour block sweep reads them: read-only loads.
+  // Offsets within the RHS's field are 32-bit.
   edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
-  const C_t<T> uc = ldro(u + (long)C * L.S + s);
+  const int si = (int)s, Si = (int)L.S;
+  const int s3[3] = {1, (int)ss[1], (int)ss[2]};
+  const C_t<T> uc = ldro(u + (C * Si + si));
   T ar = e.dre * uc.x - e.dim * uc.y;
   T ai = e.dre * uc.y + e.dim * uc.x;
 #pragma unroll
   for (int k = 0; k < 12; k++) {
-    const C_t<T> v = ldro(u + s + nbr_slot_delta<C>(k, ss, L.S));
+    const C_t<T> v = ldro(u + (si + nbr_delta32<C>(k, s3, Si)));
     ar += e.c[k] * v.x;
     ai += e.c[k] * v.y;
   }

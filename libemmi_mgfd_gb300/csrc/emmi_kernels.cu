@@ -109,13 +109,14 @@ __device__ __forceinline__ double residual_comp(const LevelView<T>& L, const C_t
                                                 const C_t<T>* f, const T* cells, const Geo<T>& G,
                                                 T wmu, const int P[3], long s, const long ss[3],
                                                 C_t<TO>* rout) {
-  C_t<T> r = f ? f[(long)C * L.S + s] : mk<T>(0, 0);  // f null: r = -A u
+  const int o = C * (int)L.S + (int)s;  // 32-bit offset within the RHS's field
+  C_t<T> r = f ? f[o] : mk<T>(0, 0);     // f null: r = -A u
   if (is_unknown<C>(L.n, P)) {
     EdgeCoef<T> e;
     const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, s, ss, e);
     r = csub<T>(r, au);
   }
-  if (rout) rout[(long)C * L.S + s] = mk<TO>((TO)r.x, (TO)r.y);
+  if (rout) rout[o] = mk<TO>((TO)r.x, (TO)r.y);
   return (double)r.x * (double)r.x + (double)r.y * (double)r.y;
 }
 
@@ -389,10 +390,10 @@ __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>
   P[D] = (TT == 0) ? s - 1 : s;
   P[A] = ta - (TT == 1 ? 1 : 0);
   P[B] = tb - (TT == 3 ? 1 : 0);
-  const long sl = slot_id(L.n, P[0], P[1], P[2]);
+  const int sl = P[0] + (L.n[0] + 1) * (P[1] + (L.n[1] + 1) * P[2]);  // 32-bit slot
   EdgeCoef<T> e;
   const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
-  const C_t<T> r = csub<T>(f[(long)C * L.S + sl], au);
+  const C_t<T> r = csub<T>(f[C * (int)L.S + sl], au);
   T band[5] = {0, 0, 0, 0, 0};
 #define LINE_ENTRY(K)                                                         \
   {                                                                           \
@@ -686,10 +687,10 @@ __device__ __forceinline__ C_t<T> row_residual(const LevelView<T>& L, const C_t<
   P[D] = (TT == 0) ? s - 1 : s;
   P[A] = ta - (TT == 1 ? 1 : 0);
   P[B] = tb - (TT == 3 ? 1 : 0);
-  const long sl = slot_id(L.n, P[0], P[1], P[2]);
+  const int sl = P[0] + (L.n[0] + 1) * (P[1] + (L.n[1] + 1) * P[2]);  // 32-bit slot
   EdgeCoef<T> e;
   const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
-  return csub<T>(f[(long)C * L.S + sl], au);
+  return csub<T>(f[C * (int)L.S + sl], au);
 }
 
 // rb[rhs][row][line] = residual of every row of one colour; y and z lines:

@@ -581,6 +581,12 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     set_err("emmi_solver_create: op==NULL needs nop==nrhs");
     return EMMI_EINVAL;
   }
+  // the stencil kernels index a level's 3 (n1+1)(n2+1)(n3+1) edge slots
+  // with 32-bit offsets
+  if (3.0 * (P->n1 + 1.0) * (P->n2 + 1.0) * (P->n3 + 1.0) >= 2147483647.0) {
+    set_err("emmi_solver_create: n=(%d,%d,%d) has 2^31 or more edge slots", P->n1, P->n2, P->n3);
+    return EMMI_EINVAL;
+  }
   emmi_solver* s = new emmi_solver();
   if (opts) s->opt = *opts; else emmi_default_options(&s->opt);
   if (s->opt.refine_every < 1) s->opt.refine_every = 3;
