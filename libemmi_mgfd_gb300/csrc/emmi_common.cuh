@@ -197,6 +197,26 @@ __device__ __forceinline__ int nbr_delta32(int k, const int ss[3], int S) {
   return o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
 }
 
+// Division by a divisor fixed for a launch, for dividends below 2^31, as a
+// multiply-high, an add and a shift: with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, u / d = (umulhi(u, m) + u) >> l
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994).  Constants come from the host.
+struct FastDiv {
+  unsigned m, l;
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  unsigned l = 0;
+  while ((1ull << l) < d) l++;
+  FastDiv f;
+  f.l = l;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned u, const FastDiv& f) {
+  return (__umulhi(u, f.m) + u) >> f.l;
+}
+
 // slot index -> node indices with 32-bit arithmetic (a level holds fewer
 // than 2^31 slots per right-hand side): one division and one modulo fewer
 // than the 64-bit decomposition, which dominated the index work

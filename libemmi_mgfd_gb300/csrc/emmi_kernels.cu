@@ -349,7 +349,7 @@ struct LineGeom {
 };
 
 template <int D>
-__device__ __forceinline__ LineGeom line_geom(const int n[3], int pa, int pb) {
+__host__ __device__ __forceinline__ LineGeom line_geom(const int n[3], int pa, int pb) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   LineGeom g;
   g.fa = pa ? 1 : 2;
@@ -374,6 +374,39 @@ __device__ __forceinline__ bool line_item(const LineGeom& g, long id, long& l, i
     const unsigned u = (unsigned)id, nl = (unsigned)g.nl;
     const unsigned q = u / nl;
     l = u - q * nl;
+    s = 1 + (int)q;
+  }
+  return true;
+}
+
+// the divisors of a colour's thread decode (one launch): rows x items
+// (x-line residual), the item-per-line divisor of line_item and the lines
+// per transverse direction
+struct LineDiv {
+  unsigned items;
+  FastDiv rows, item, la;
+};
+template <int D>
+LineDiv line_div(const int n[3], int pa, int pb) {
+  const LineGeom g = line_geom<D>(n, pa, pb);
+  LineDiv v;
+  v.items = (unsigned)(g.nl * g.nd);
+  v.rows = make_fastdiv(v.items > 0 ? v.items : 1);
+  v.item = make_fastdiv((unsigned)(D == 0 ? g.nd : (g.nl > 0 ? g.nl : 1)));
+  v.la = make_fastdiv((unsigned)(g.la > 0 ? g.la : 1));
+  return v;
+}
+// line_item with the launch's divisor
+template <int D>
+__device__ __forceinline__ bool line_item_fd(const LineGeom& g, const LineDiv& v, unsigned id,
+                                             long& l, int& s) {
+  if (id >= v.items) return false;
+  const unsigned q = fdiv(id, v.item);
+  if (D == 0) {  // rows of an x-line are contiguous in memory
+    l = q;
+    s = 1 + (int)(id - q * (unsigned)g.nd);
+  } else {  // neighbouring lines (consecutive i) are contiguous
+    l = id - q * (unsigned)g.nl;
     s = 1 + (int)q;
   }
   return true;
@@ -697,25 +730,24 @@ __device__ __forceinline__ C_t<T> row_residual(const LevelView<T>& L, const C_t<
 // a thread per (line, node) and its five rows; x lines: a thread per
 // (row type, line, node), row type slowest
 template <typename T, int D>
-__global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb,
+__global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb, LineDiv dv,
                                                   C_t<T>* __restrict__ rb) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   const int rhs = blockIdx.y;
   if (L.active && !L.active[rhs]) return;
   const LineGeom g = line_geom<D>(L.n, pa, pb);
-  const long items = g.nl * g.nd;
-  long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
   int rt = 0;
   if (D == 0) {
-    rt = (int)((unsigned)id / (unsigned)items);
+    rt = (int)fdiv(id, dv.rows);
     if (rt >= 5) return;
-    id -= rt * items;
+    id -= (unsigned)rt * dv.items;
   }
   long l;
   int s;
-  if (!line_item<D>(g, id, l, s)) return;
+  if (!line_item_fd<D>(g, dv, id, l, s)) return;
   if (D == 0 && rt > 0 && s == g.nd) return;
-  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const unsigned lq = fdiv((unsigned)l, dv.la);
   const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
@@ -935,15 +967,15 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_subst(const int* __restr
 
 // u += x from rb[rhs][row][line]
 template <typename T, int D>
-__global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, int pb,
+__global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, int pb, LineDiv dv,
                                                        const C_t<T>* __restrict__ rb) {
   const int rhs = blockIdx.y;
   if (L.active && !L.active[rhs]) return;
   const LineGeom g = line_geom<D>(L.n, pa, pb);
   long l;
   int s;
-  if (!line_item<D>(g, blockIdx.x * (long)blockDim.x + threadIdx.x, l, s)) return;
-  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  if (!line_item_fd<D>(g, dv, blockIdx.x * blockDim.x + threadIdx.x, l, s)) return;
+  const unsigned lq = fdiv((unsigned)l, dv.la);
   const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
   C_t<T>* u = L.u + (long)rhs * 3 * L.S;
   const C_t<T>* x = rb + (long)rhs * g.m * g.nl + l;
@@ -981,10 +1013,11 @@ static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, con
   const int m = 5 * L.n[D] - 4;
   dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
   dim3 gr((unsigned)(((D == 0 ? 5 : 1) * items + 255) / 256), L.nrhs);
-  k_line_rhs<T, D><<<gr, 256, 0, st>>>(L, pa, pb, rb);
+  const LineDiv dv = line_div<D>(L.n, pa, pb);
+  k_line_rhs<T, D><<<gr, 256, 0, st>>>(L, pa, pb, dv, rb);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
   k_line_subst<T><<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m, fac, rb);
-  k_line_apply_rb<T, D><<<g1, 256, 0, st>>>(L, pa, pb, rb);
+  k_line_apply_rb<T, D><<<g1, 256, 0, st>>>(L, pa, pb, dv, rb);
 }
 
 template <typename T, int D>

@@ -53,3 +53,14 @@ def test_reference_entry_points_are_declared():
               "extract_emf_data", "extract_electric_field", "extract_magnetic_field",
               "build_gradient"):
         assert n in names, n
+
+
+def test_create_refuses_grids_beyond_32_bit_offsets(built):
+    """The stencil kernels use 32-bit slot offsets: emmi_solver_create turns
+    down a grid with 2^31 or more edge slots before it touches the device."""
+    import numpy as np
+    from libemmi_mgfd_gb300 import gpu as G
+    n = (1300, 1300, 1300)
+    x = [np.arange(v + 1, dtype=np.float32) for v in n]
+    with pytest.raises(G.EmmiError, match="2\\^31"):
+        G.Solver(n, *x, np.zeros((1, 4, 1), np.float32), np.ones(1, np.float32))
