@@ -120,6 +120,8 @@ __device__ __forceinline__ double residual_comp(const LevelView<T>& L, const C_t
   return (double)r.x * (double)r.x + (double)r.y * (double)r.y;
 }
 
+// a thread per (component, slot), the component = blockIdx.z: one edge
+// equation per thread keeps more independent loads in flight than three
 template <typename T, typename TO>
 __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __restrict__ rout,
                                                   double* __restrict__ norm2) {
@@ -138,16 +140,18 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
     const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
     const T wmu = L.wmu[rhs];
     C_t<TO>* ro = rout ? rout + (long)rhs * 3 * L.S : nullptr;
-    acc += residual_comp<T, TO, 0>(L, u, f, cells, G, wmu, P, s, ss, ro);
-    acc += residual_comp<T, TO, 1>(L, u, f, cells, G, wmu, P, s, ss, ro);
-    acc += residual_comp<T, TO, 2>(L, u, f, cells, G, wmu, P, s, ss, ro);
+    switch (blockIdx.z) {
+      case 0: acc = residual_comp<T, TO, 0>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
+      case 1: acc = residual_comp<T, TO, 1>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
+      default: acc = residual_comp<T, TO, 2>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
+    }
   }
   if (norm2) block_add(acc, norm2 + rhs);
 }
 
 template <typename T, typename TO>
 void launch_residual(const LevelView<T>& L, C_t<TO>* rout, double* norm2, cudaStream_t st) {
-  dim3 grid((unsigned)((L.S + 255) / 256), L.nrhs);
+  dim3 grid((unsigned)((L.S + 255) / 256), L.nrhs, 3);
   k_residual<T, TO><<<grid, 256, 0, st>>>(L, rout, norm2);
 }
 
