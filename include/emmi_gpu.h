@@ -72,10 +72,12 @@ typedef struct {
   int krylov;       /* MIXED: 0 = stationary FP64 refinement of complex64
                        cycles; k > 0 = FP64 FGMRES(k) (k <= 12) with one
                        complex64 cycle as its preconditioner (0)           */
-  int line_factors; /* MIXED: 1 = factor every line once per (operator,
+  int line_factors; /* MIXED: factor every line once per (operator,
                        frequency) at set-up and keep the factors, when they
-                       fit in half the free device memory; 0 = factor in
-                       every sweep (1)                                     */
+                       fit in half the free device memory: 2 = L in fp16,
+                       1/d in fp32 (fp32 throughout if an L value leaves
+                       the fp16 range), 1 = fp32; 0 = factor in every
+                       sweep (2)                                           */
 } emmi_options;
 
 typedef struct {

@@ -17,8 +17,11 @@
 // (checked by tests/test_coloring.py), so a colour is one parallel launch.
 #include "emmi_kernels.cuh"
 
+#include <cuda_fp16.h>
+
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 
 namespace emmi {
 
@@ -792,13 +795,50 @@ __device__ __forceinline__ void cp_async_c(C_t<T>* smem, const C_t<T>* gmem) {
   else cp_async16(smem, gmem);
 }
 
+// Stored-factor formats: kFacF32 keeps the 12 fp32 values per row of
+// k_line_solve; kFacF16 keeps the five L values per row as fp16 complex
+// (20 bytes) and 1/d as fp32 complex (8 bytes), 28 instead of 48 bytes per
+// row for the substitution to stream.  A group's kFacF16 block of m rows x
+// nl lines: LA [m][nl] uint4 (L1..L4), LB [m][nl] half2 (L5), ID [m][nl]
+// float2, each part starting on 16 bytes.
+__host__ __device__ inline long round4(long v) { return (v + 3) / 4 * 4; }
+__host__ __device__ inline long half_fac_elems(int m, long nl) {
+  return round4(4 * m * nl) + round4(m * nl) + round4(2 * m * nl);
+}
+struct HalfFac {
+  uint4* la;
+  __half2* lb;
+  float2* id;
+};
+__host__ __device__ inline HalfFac half_fac(const float* g, int m, long nl) {
+  float* b = const_cast<float*>(g);
+  HalfFac h;
+  h.la = reinterpret_cast<uint4*>(b);
+  h.lb = reinterpret_cast<__half2*>(b + round4(4 * m * nl));
+  h.id = reinterpret_cast<float2*>(b + round4(4 * m * nl) + round4(m * nl));
+  return h;
+}
+__device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+__device__ __forceinline__ float2 u2f2(uint32_t u) {
+  return __half22float2(*reinterpret_cast<__half2*>(&u));
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
 // Factors of every line of one colour, for group blockIdx.y of the chunk:
 // the forward elimination of k_line_solve on records assembled in buf
-// (their right-hand sides unused), factors to fac (same record layout).
-template <typename T>
-__global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m,
+// (their right-hand sides unused), factors to fac + grp * gstride:
+//   FMT 0 (kFacF32): the record layout, 12 values per row;
+//   FMT 1 (kFacF16, T = float): L(p+i, p), i = 1..5, rounded to fp16 in
+//   planes LA (i = 1..4) and LB (i = 5), 1/d_p in fp32 (ID); an L value
+//   outside the fp16 range (or not finite) sets *ovf.
+template <typename T, int FMT>
+__global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m, long gstride,
                                                                const T* __restrict__ buf,
-                                                               T* __restrict__ fac) {
+                                                               T* __restrict__ fac,
+                                                               int* __restrict__ ovf) {
   using V = typename Vec16<T>::V;
   constexpr int NP = kPlanes<T>;
   __shared__ V ring[kRing][NP][kSolveThreads];
@@ -807,8 +847,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m,
   const long l = blockIdx.x * (long)blockDim.x + tid;
   if (l >= nl) return;
   const V* base = reinterpret_cast<const V*>(buf) + (long)grp * m * NP * nl + l;
-  V* fout = reinterpret_cast<V*>(fac) + (long)grp * m * NP * nl + l;
+  V* fout = reinterpret_cast<V*>(fac + (long)grp * gstride) + l;
   const long rs = NP * nl;
+  HalfFac hf{};
+  if constexpr (FMT == kFacF16) hf = half_fac(fac + (long)grp * gstride, m, nl);
+  bool over = false;
   auto issue = [&](int row) {
     const V* src = base + (long)row * rs;
     const int slot = row % kRing;
@@ -852,15 +895,28 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m,
     }
     const int piv = row - 5;
     if (piv >= 0) {
-      T o[kRec];
+      if constexpr (FMT == kFacF32) {
+        T o[kRec];
 #pragma unroll
-      for (int i = 1; i < 6; i++) {
-        o[2 * (i - 1)] = lq[i].x;
-        o[2 * (i - 1) + 1] = lq[i].y;
+        for (int i = 1; i < 6; i++) {
+          o[2 * (i - 1)] = lq[i].x;
+          o[2 * (i - 1) + 1] = lq[i].y;
+        }
+        o[10] = id.x;
+        o[11] = id.y;
+        rec_put<T>(fout + (long)piv * rs, nl, o);
+      } else {
+        __half2 h[5];
+#pragma unroll
+        for (int i = 1; i < 6; i++) {
+          over |= !(fabsf(lq[i].x) <= 65504.f && fabsf(lq[i].y) <= 65504.f);
+          h[i - 1] = __floats2half2_rn(lq[i].x, lq[i].y);
+        }
+        const long o = (long)piv * nl + l;
+        hf.la[o] = make_uint4(h2u(h[0]), h2u(h[1]), h2u(h[2]), h2u(h[3]));
+        hf.lb[o] = h[4];
+        hf.id[o] = make_float2(id.x, id.y);
       }
-      o[10] = id.x;
-      o[11] = id.y;
-      rec_put<T>(fout + (long)piv * rs, nl, o);
     }
 #pragma unroll
     for (int i = 0; i < 5; i++) {
@@ -869,6 +925,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m,
     }
   }
   cp_async_wait<0>();
+  if (over) atomicOr(ovf, 1);
 }
 
 // Substitution with stored factors (group grp[rhs]): rb holds the rows'
@@ -969,6 +1026,100 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_subst(const int* __restr
   cp_async_wait<0>();
 }
 
+// The same substitution with kFacF16 factors of group grp[rhs] (gstride
+// values per group): the forward pass streams LA, LB and ID, the backward
+// pass LA and LB; the fp16 values are widened to fp32 and the arithmetic is
+// k_line_subst's.
+__global__ void __launch_bounds__(kSolveThreads) k_line_subst_h(const int* __restrict__ active,
+                                                                const int* __restrict__ grp,
+                                                                long nl, int m, long gstride,
+                                                                const float* __restrict__ fac,
+                                                                float2* __restrict__ rb) {
+  __shared__ uint4 ra[kRing][kSolveThreads];
+  __shared__ uint32_t rl5[kRing][kSolveThreads];
+  __shared__ float2 rd[kRing][kSolveThreads];
+  __shared__ float2 rring[kRing][kSolveThreads];
+  const int rhs = blockIdx.y;
+  if (active && !active[rhs]) return;
+  const int tid = threadIdx.x;
+  const long l = blockIdx.x * (long)blockDim.x + tid;
+  if (l >= nl) return;
+  const HalfFac hf = half_fac(fac + (long)grp[rhs] * gstride, m, nl);
+  float2* rr = rb + (long)rhs * m * nl + l;
+  auto issue_l = [&](int row) {
+    const int slot = row % kRing;
+    cp_async16(&ra[slot][tid], hf.la + (long)row * nl + l);
+    cp_async4(&rl5[slot][tid], hf.lb + (long)row * nl + l);
+  };
+  auto take_l = [&](int row, float2 (&v)[5]) {
+    const int slot = row % kRing;
+    const uint4 a = ra[slot][tid];
+    v[0] = u2f2(a.x);
+    v[1] = u2f2(a.y);
+    v[2] = u2f2(a.z);
+    v[3] = u2f2(a.w);
+    v[4] = u2f2(rl5[slot][tid]);
+  };
+  // forward: at step `row` the residual of row `row` arrives and pivot
+  // row-5 is eliminated with its stored factors
+  float2 y[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) y[i] = make_float2(0.f, 0.f);
+  auto issue_fwd = [&](int q) {
+    if (q < m) cp_async8(&rring[q % kRing][tid], rr + (long)q * nl);
+    const int p = q - 5;
+    if (p >= 0 && p < m) {
+      issue_l(p);
+      cp_async8(&rd[p % kRing][tid], hf.id + (long)p * nl + l);
+    }
+    cp_async_commit();
+  };
+  for (int p = 0; p < kRing - 1; p++) issue_fwd(p);
+  for (int row = 0; row < m + 5; row++) {
+    issue_fwd(row + kRing - 1);
+    cp_async_wait<kRing - 1>();
+    y[5] = row < m ? rring[row % kRing][tid] : make_float2(0.f, 0.f);
+    const int piv = row - 5;
+    if (piv >= 0) {
+      float2 v[5];
+      take_l(piv, v);
+#pragma unroll
+      for (int i = 1; i < 6; i++) y[i] = cfms<float>(y[i], v[i - 1], y[0]);
+      rr[(long)piv * nl] = cmul<float>(y[0], rd[piv % kRing][tid]);  // z
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) y[i] = y[i + 1];
+  }
+  cp_async_wait<0>();
+  __threadfence_block();  // z just stored is read back below
+  // backward: x_k = z_k - sum_i L(k+i, k) x_{k+i}
+  float2 xw[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) xw[i] = make_float2(0.f, 0.f);
+  auto issue_bwd = [&](int q) {
+    if (q >= 0) {
+      issue_l(q);
+      cp_async8(&rring[q % kRing][tid], rr + (long)q * nl);
+    }
+    cp_async_commit();
+  };
+  for (int p = 0; p < kRing - 1; p++) issue_bwd(m - 1 - p);
+  for (int row = m - 1; row >= 0; row--) {
+    issue_bwd(row - (kRing - 1));
+    cp_async_wait<kRing - 1>();
+    float2 v[5];
+    take_l(row, v);
+    float2 x = rring[row % kRing][tid];
+#pragma unroll
+    for (int i = 0; i < 5; i++) x = cfms<float>(x, v[i], xw[i]);
+#pragma unroll
+    for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
+    xw[0] = x;
+    rr[(long)row * nl] = x;
+  }
+  cp_async_wait<0>();
+}
+
 // u += x from rb[rhs][row][line]
 template <typename T, int D>
 __global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, int pb, LineDiv dv,
@@ -995,21 +1146,29 @@ __global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, i
 }
 
 template <typename T, int D>
-static void line_factor_d(const LevelView<T>& L, int color, T* buf, T* fac, cudaStream_t st) {
+static void line_factor_d(const LevelView<T>& L, int color, T* buf, T* fac, int fmt, int* ovf,
+                          cudaStream_t st) {
   const int pa = color & 1, pb = (color >> 1) & 1;
   const long nl = line_count(L.n, D, color);
   if (nl == 0) return;
   const long items = nl * L.n[D];
   const int m = 5 * L.n[D] - 4;
+  const long gstride = line_factor_elems(L.n, D, color, fmt);
   dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
   k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
-  k_line_factor<T><<<g2, kSolveThreads, 0, st>>>(nl, m, buf, fac);
+  if constexpr (std::is_same<T, float>::value) {
+    if (fmt == kFacF16) {
+      k_line_factor<T, kFacF16><<<g2, kSolveThreads, 0, st>>>(nl, m, gstride, buf, fac, ovf);
+      return;
+    }
+  }
+  k_line_factor<T, kFacF32><<<g2, kSolveThreads, 0, st>>>(nl, m, gstride, buf, fac, ovf);
 }
 
 template <typename T, int D>
 static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, const int* grp,
-                             C_t<T>* rb, cudaStream_t st) {
+                             C_t<T>* rb, int fmt, cudaStream_t st) {
   const int pa = color & 1, pb = (color >> 1) & 1;
   const long nl = line_count(L.n, D, color);
   if (nl == 0) return;
@@ -1020,7 +1179,15 @@ static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, con
   const LineDiv dv = line_div<D>(L.n, pa, pb);
   k_line_rhs<T, D><<<gr, 256, 0, st>>>(L, pa, pb, dv, rb);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
-  k_line_subst<T><<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m, fac, rb);
+  bool done = false;
+  if constexpr (std::is_same<T, float>::value) {
+    if (fmt == kFacF16) {
+      k_line_subst_h<<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m,
+                                                   line_factor_elems(L.n, D, color, fmt), fac, rb);
+      done = true;
+    }
+  }
+  if (!done) k_line_subst<T><<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m, fac, rb);
   k_line_apply_rb<T, D><<<g1, 256, 0, st>>>(L, pa, pb, dv, rb);
 }
 
@@ -1054,7 +1221,13 @@ void init_line_kernels() {
                          cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_line_subst<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_factor<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(k_line_subst_h, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_factor<float, kFacF32>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_factor<float, kFacF16>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
   });
 }
@@ -1068,25 +1241,27 @@ void launch_line_sweep(const LevelView<T>& L, int d, int color, C_t<T>* scratch,
   else line_sweep_d<T, 2>(L, color, buf, st);
 }
 
-long line_factor_elems(const int n[3], int d, int color) {
-  return (long)(5 * n[d] - 4) * line_count(n, d, color) * kRec;
+long line_factor_elems(const int n[3], int d, int color, int fmt) {
+  const int m = 5 * n[d] - 4;
+  const long nl = line_count(n, d, color);
+  return fmt == kFacF16 ? half_fac_elems(m, nl) : (long)m * nl * kRec;
 }
 
 template <typename T>
 void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
-                        cudaStream_t st) {
+                        int fmt, int* ovf, cudaStream_t st) {
   T* buf = reinterpret_cast<T*>(scratch);
-  if (d == 0) line_factor_d<T, 0>(L, color, buf, fac, st);
-  else if (d == 1) line_factor_d<T, 1>(L, color, buf, fac, st);
-  else line_factor_d<T, 2>(L, color, buf, fac, st);
+  if (d == 0) line_factor_d<T, 0>(L, color, buf, fac, fmt, ovf, st);
+  else if (d == 1) line_factor_d<T, 1>(L, color, buf, fac, fmt, ovf, st);
+  else line_factor_d<T, 2>(L, color, buf, fac, fmt, ovf, st);
 }
 
 template <typename T>
 void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
-                           C_t<T>* rb, cudaStream_t st) {
-  if (d == 0) line_sweep_fac_d<T, 0>(L, color, fac, grp, rb, st);
-  else if (d == 1) line_sweep_fac_d<T, 1>(L, color, fac, grp, rb, st);
-  else line_sweep_fac_d<T, 2>(L, color, fac, grp, rb, st);
+                           C_t<T>* rb, int fmt, cudaStream_t st) {
+  if (d == 0) line_sweep_fac_d<T, 0>(L, color, fac, grp, rb, fmt, st);
+  else if (d == 1) line_sweep_fac_d<T, 1>(L, color, fac, grp, rb, fmt, st);
+  else line_sweep_fac_d<T, 2>(L, color, fac, grp, rb, fmt, st);
 }
 
 // ------------------------------------------------------------ point sweep
@@ -1407,9 +1582,9 @@ void launch_zero(C_t<T>* p, long n, cudaStream_t st) {
 EMMI_INST(float)
 EMMI_INST(double)
 template void launch_line_factor<float>(const LevelView<float>&, int, int, C_t<float>*, float*,
-                                        cudaStream_t);
+                                        int, int*, cudaStream_t);
 template void launch_line_sweep_fac<float>(const LevelView<float>&, int, int, const float*,
-                                           const int*, C_t<float>*, cudaStream_t);
+                                           const int*, C_t<float>*, int, cudaStream_t);
 template void launch_residual<float, float>(const LevelView<float>&, C_t<float>*, double*, cudaStream_t);
 template void launch_residual<double, double>(const LevelView<double>&, C_t<double>*, double*, cudaStream_t);
 template void launch_residual<double, float>(const LevelView<double>&, C_t<float>*, double*, cudaStream_t);

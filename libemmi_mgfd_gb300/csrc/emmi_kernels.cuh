@@ -33,18 +33,21 @@ long line_count(const int n[3], int d, int color);
 long line_scratch_elems(const int n[3], int d, int nrhs);
 
 // stored LDL^T factors of the lines of one colour along d: T values per
-// operator group; launch_line_factor fills them for the L.nrhs groups of L
-// (L.op / L.wmu per group, u and f unused) through the record scratch into
-// fac + g * line_factor_elems; launch_line_sweep_fac then sweeps RHS r with
-// the factors of group grp[r], rb holding (5 n_d - 4) * lines complex values
-// per RHS
-long line_factor_elems(const int n[3], int d, int color);
+// operator group in format fmt (0: fp32 records, 12 values per row; 1: fp16
+// L and fp32 1/d, 7 values per row); launch_line_factor fills them for the
+// L.nrhs groups of L (L.op / L.wmu per group, u and f unused) through the
+// record scratch into fac + g * line_factor_elems and sets *ovf when an L
+// value does not fit fp16 (format 1); launch_line_sweep_fac then sweeps RHS
+// r with the factors of group grp[r], rb holding (5 n_d - 4) * lines complex
+// values per RHS
+constexpr int kFacF32 = 0, kFacF16 = 1;
+long line_factor_elems(const int n[3], int d, int color, int fmt);
 template <typename T>
 void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
-                        cudaStream_t st);
+                        int fmt, int* ovf, cudaStream_t st);
 template <typename T>
 void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
-                           C_t<T>* rb, cudaStream_t st);
+                           C_t<T>* rb, int fmt, cudaStream_t st);
 
 template <typename T>
 void launch_point_sweep(const LevelView<T>& L, int color, cudaStream_t st);

@@ -232,8 +232,20 @@ int emmi_solver::alloc(void** p, size_t b) {
     return EMMI_ENOMEM;
   }
   allocs.push_back(*p);
+  alloc_bytes.push_back(b);
   bytes += b;
   return EMMI_OK;
+}
+
+void emmi_solver::release(void* p) {
+  for (size_t i = 0; i < allocs.size(); i++)
+    if (allocs[i] == p) {
+      cudaFree(p);
+      bytes -= alloc_bytes[i];
+      allocs.erase(allocs.begin() + i);
+      alloc_bytes.erase(alloc_bytes.begin() + i);
+      return;
+    }
 }
 
 template <>
@@ -289,7 +301,7 @@ static void line_colour(emmi_solver* s, int h, int l, int d, int col, const Leve
       const long off = s->fac_off[l == 0 ? 0 : h][l][d][col];
       if (off >= 0) {
         launch_line_sweep_fac<float>(W, d, col, s->d_fac + off, s->d_grp + r0,
-                                     (C_t<float>*)s->scratch, s->st);
+                                     (C_t<float>*)s->scratch, s->fac_fmt, s->st);
         return;
       }
     }
@@ -450,70 +462,94 @@ static int build_line_factors(emmi_solver* s) {
     grp[r] = g;
   }
   const int ng = (int)gop.size();
-  for (int h = 0; h < 3; h++)
-    for (int l = 0; l < emmi::kMaxLev; l++)
-      for (int d = 0; d < 3; d++)
-        for (int c = 0; c < 4; c++) s->fac_off[h][l][d][c] = -1;
-  // level 0 is the same in every hierarchy: its blocks live under h = 0
-  long total = 0;
-  for (int h = 0; h < 3; h++)
-    for (int l = 0; l + 1 < s->lmax; l++)
-      for (int d = 0; d < 3; d++) {
-        if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
-        const int hb = l == 0 ? 0 : h;
-        if (s->fac_off[hb][l][d][0] >= 0) continue;
-        for (int c = 0; c < 4; c++) {
-          s->fac_off[hb][l][d][c] = total;
-          total += (long)ng * line_factor_elems(s->hier[h][l].n, d, c);
-        }
-      }
-  if (total == 0) return EMMI_OK;
-  size_t freeb = 0, totb = 0;
-  CK(cudaMemGetInfo(&freeb, &totb));
-  const size_t bytes = (size_t)total * sizeof(float);
-  if (bytes > freeb / 2) return EMMI_OK;  // factor in every sweep instead
+  // fp16 L (the default, line_factors = 2) unless a value leaves its range;
+  // then every factor is recomputed in fp32
+  int fmt = s->opt.line_factors == 2 ? kFacF16 : kFacF32;
+  int* d_ovf = nullptr;
   int rc;
-  if ((rc = s->alloc((void**)&s->d_fac, bytes)) != EMMI_OK) return rc;
-  if ((rc = s->alloc((void**)&s->d_grp, nrhs * sizeof(int))) != EMMI_OK) return rc;
-  if ((rc = s->alloc((void**)&s->d_gop, ng * sizeof(int))) != EMMI_OK) return rc;
-  if ((rc = s->alloc((void**)&s->d_gwmu, ng * sizeof(float))) != EMMI_OK) return rc;
-  CK(cudaMemcpyAsync(s->d_grp, grp.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, s->st));
-  CK(cudaMemcpyAsync(s->d_gop, gop.data(), ng * sizeof(int), cudaMemcpyHostToDevice, s->st));
-  CK(cudaMemcpyAsync(s->d_gwmu, gw.data(), ng * sizeof(float), cudaMemcpyHostToDevice, s->st));
-  s->ngroups = ng;
-  s->fac_bytes = bytes;
-  // factor every block once: records assembled into the scratch for `chunk`
-  // groups at a time (u and f of the level are read but their residual is
-  // not used)
-  std::vector<long> done;
-  for (int h = 0; h < 3; h++)
-    for (int l = 0; l + 1 < s->lmax; l++)
-      for (int d = 0; d < 3; d++) {
-        if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
-        const int hb = l == 0 ? 0 : h;
-        const long off0 = s->fac_off[hb][l][d][0];
-        if (std::find(done.begin(), done.end(), off0) != done.end()) continue;
-        done.push_back(off0);
-        LevelView<float> V = s->view<float>(h, l);
-        V.op = s->d_gop;
-        V.wmu = s->d_gwmu;
-        V.active = nullptr;
-        for (int c = 0; c < 4; c++) {
-          const long per = line_factor_elems(s->hier[h][l].n, d, c);
-          for (int g0 = 0; g0 < ng; g0 += s->chunk) {
-            LevelView<float> W = V;
-            W.nrhs = std::min(s->chunk, ng - g0);
-            W.u += (long)g0 * 3 * V.S;
-            W.f += (long)g0 * 3 * V.S;
-            W.op += g0;
-            W.wmu += g0;
-            launch_line_factor<float>(W, d, c, (C_t<float>*)s->scratch,
-                                      s->d_fac + s->fac_off[hb][l][d][c] + (long)g0 * per, s->st);
+  if ((rc = s->alloc((void**)&d_ovf, sizeof(int))) != EMMI_OK) return rc;
+  for (;;) {
+    for (int h = 0; h < 3; h++)
+      for (int l = 0; l < emmi::kMaxLev; l++)
+        for (int d = 0; d < 3; d++)
+          for (int c = 0; c < 4; c++) s->fac_off[h][l][d][c] = -1;
+    // level 0 is the same in every hierarchy: its blocks live under h = 0
+    long total = 0;
+    for (int h = 0; h < 3; h++)
+      for (int l = 0; l + 1 < s->lmax; l++)
+        for (int d = 0; d < 3; d++) {
+          if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
+          const int hb = l == 0 ? 0 : h;
+          if (s->fac_off[hb][l][d][0] >= 0) continue;
+          for (int c = 0; c < 4; c++) {
+            s->fac_off[hb][l][d][c] = total;
+            total += (long)ng * line_factor_elems(s->hier[h][l].n, d, c, fmt);
           }
         }
-      }
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(s->st));
+    if (total == 0) return EMMI_OK;
+    size_t freeb = 0, totb = 0;
+    CK(cudaMemGetInfo(&freeb, &totb));
+    const size_t bytes = (size_t)total * sizeof(float);
+    if (bytes > freeb / 2) return EMMI_OK;  // factor in every sweep instead
+    if ((rc = s->alloc((void**)&s->d_fac, bytes)) != EMMI_OK) return rc;
+    if (!s->d_grp) {
+      if ((rc = s->alloc((void**)&s->d_grp, nrhs * sizeof(int))) != EMMI_OK) return rc;
+      if ((rc = s->alloc((void**)&s->d_gop, ng * sizeof(int))) != EMMI_OK) return rc;
+      if ((rc = s->alloc((void**)&s->d_gwmu, ng * sizeof(float))) != EMMI_OK) return rc;
+      CK(cudaMemcpyAsync(s->d_grp, grp.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice,
+                         s->st));
+      CK(cudaMemcpyAsync(s->d_gop, gop.data(), ng * sizeof(int), cudaMemcpyHostToDevice, s->st));
+      CK(cudaMemcpyAsync(s->d_gwmu, gw.data(), ng * sizeof(float), cudaMemcpyHostToDevice,
+                         s->st));
+    }
+    CK(cudaMemsetAsync(d_ovf, 0, sizeof(int), s->st));
+    s->ngroups = ng;
+    s->fac_bytes = bytes;
+    // factor every block once: records assembled into the scratch for
+    // `chunk` groups at a time (u and f of the level are read but their
+    // residual is not used)
+    std::vector<long> done;
+    for (int h = 0; h < 3; h++)
+      for (int l = 0; l + 1 < s->lmax; l++)
+        for (int d = 0; d < 3; d++) {
+          if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
+          const int hb = l == 0 ? 0 : h;
+          const long off0 = s->fac_off[hb][l][d][0];
+          if (std::find(done.begin(), done.end(), off0) != done.end()) continue;
+          done.push_back(off0);
+          LevelView<float> V = s->view<float>(h, l);
+          V.op = s->d_gop;
+          V.wmu = s->d_gwmu;
+          V.active = nullptr;
+          for (int c = 0; c < 4; c++) {
+            const long per = line_factor_elems(s->hier[h][l].n, d, c, fmt);
+            for (int g0 = 0; g0 < ng; g0 += s->chunk) {
+              LevelView<float> W = V;
+              W.nrhs = std::min(s->chunk, ng - g0);
+              W.u += (long)g0 * 3 * V.S;
+              W.f += (long)g0 * 3 * V.S;
+              W.op += g0;
+              W.wmu += g0;
+              launch_line_factor<float>(W, d, c, (C_t<float>*)s->scratch,
+                                        s->d_fac + s->fac_off[hb][l][d][c] + (long)g0 * per, fmt,
+                                        d_ovf, s->st);
+            }
+          }
+        }
+    CK(cudaGetLastError());
+    int ovf = 0;
+    CK(cudaMemcpyAsync(&ovf, d_ovf, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (fmt == kFacF16 && ovf) {
+      s->release(s->d_fac);
+      s->d_fac = nullptr;
+      fmt = kFacF32;
+      continue;
+    }
+    break;
+  }
+  s->release(d_ovf);
+  s->fac_fmt = fmt;
   s->fac_on = true;
   return EMMI_OK;
 }
@@ -558,7 +594,7 @@ void emmi_default_options(emmi_options* o) {
   o->use_graphs = 1;
   o->verb = 0;
   o->krylov = 0;
-  o->line_factors = 1;
+  o->line_factors = 2;
 }
 
 int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_options* opts) {

@@ -32,6 +32,7 @@ struct emmi_solver {
 
   // device memory
   std::vector<void*> allocs;
+  std::vector<size_t> alloc_bytes;  // sizes of allocs, same order
   size_t bytes = 0;
   int* d_op = nullptr;
   int* d_active = nullptr;  // cycling RHS
@@ -75,6 +76,7 @@ struct emmi_solver {
   // line per group, in blocks per (hierarchy, level, direction, colour) at
   // float offsets fac_off (-1: none; level 0 is shared by the hierarchies)
   bool fac_on = false;
+  int fac_fmt = 0;          // 0: fp32 records; 1: fp16 L with fp32 1/d
   int ngroups = 0;
   int* d_grp = nullptr;     // [nrhs] group of each RHS
   int* d_gop = nullptr;     // [ngroups] operator of each group
@@ -127,6 +129,7 @@ struct emmi_solver {
   template <typename T> void emit_residual0(int want, int& cur);
   template <typename T> int build_graphs();
   int alloc(void** p, size_t b);
+  void release(void* p);  // frees one allocation made by alloc
 };
 
 // one part of a cycle on hierarchy h (graph launch or direct emission)

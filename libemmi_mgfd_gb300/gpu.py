@@ -105,7 +105,7 @@ class Options:
     use_graphs: int = 1
     verb: int = 0
     krylov: int = 0
-    line_factors: int = 1
+    line_factors: int = 2
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,

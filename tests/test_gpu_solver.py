@@ -216,3 +216,34 @@ def test_stored_line_factors_give_the_same_iterates(golden):
     for r in range(3):
         assert rel_err(out[1][0][r], out[0][0][r], sea) < 1e-6
         assert rel_err(out[1][1][r], out[0][1][r]) < 1e-6
+
+
+@gpu
+def test_fp16_line_factors_converge_like_fp32(golden):
+    """Stored factors with L in fp16 (the default) against fp32 factors: the
+    substitution reads 28 instead of 48 bytes per row; the smoother's line
+    solves change by the fp16 rounding of L, the FP64 refinement keeps the
+    answer.  Cycle counts within 10 % and the same converged fields."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"]])
+    oms = np.array([om, om, 0.5 * om], np.float32)
+    out = {}
+    for lf in (2, 1):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
+                     op=np.zeros(3, np.int32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=120, tol=1e-8,
+                                       sigma_floor=2e-4, line_factors=lf))
+        x, h, st = s.solve(bs)
+        out[lf] = (x, h, st)
+        s.close()
+    for lf in (2, 1):
+        print("line_factors", lf, [(q["status"], q["cycles"], q["rel"]) for q in out[lf][2]])
+    sea = below_sea_mask(n, g["x3"])
+    for r in range(3):
+        assert out[2][2][r]["status"] == "ok" and out[1][2][r]["status"] == "ok"
+        c2, c1 = out[2][2][r]["cycles"], out[1][2][r]["cycles"]
+        assert abs(c2 - c1) <= max(2, c1 // 10), (c2, c1)
+        assert rel_err(out[2][0][r], out[1][0][r], sea) < 1e-6
+        assert rel_err(out[2][1][r], out[1][1][r]) < 1e-6
