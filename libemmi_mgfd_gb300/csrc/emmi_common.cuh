@@ -78,6 +78,10 @@ template <typename T> __device__ __forceinline__ int op_of(const LevelView<T>& L
 __host__ __device__ __forceinline__ long slot_id(const int n[3], int i, int j, int k) {
   return i + (long)(n[0] + 1) * (j + (long)(n[1] + 1) * k);
 }
+// 32-bit slot index (a level has fewer than 2^31 edge slots)
+__host__ __device__ __forceinline__ int slot_id32(const int n[3], int i, int j, int k) {
+  return i + (n[0] + 1) * (j + (n[1] + 1) * k);
+}
 __host__ __device__ __forceinline__ long cell_id(const int n[3], int i, int j, int k) {
   return i + (long)n[0] * (j + (long)n[1] * k);
 }

@@ -1425,7 +1425,7 @@ __device__ __forceinline__ C_t<T> restrict_comp(const LevelView<T>& F, const Lev
         P[C] = fc;
         P[t1] = i1[a];
         P[t2] = i2[b];
-        const C_t<T> v = rf[(long)C * F.S + slot_id(F.n, P[0], P[1], P[2])];
+        const C_t<T> v = rf[C * (int)F.S + slot_id32(F.n, P[0], P[1], P[2])];
         const T w = w1[a] * w2[b];
         ar += w * v.x;
         ai += w * v.y;
@@ -1446,21 +1446,24 @@ __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C
   int Cn[3];
   slot_nodes(s, n0, n1, Cn);
   const C_t<T>* rf = F.r + (long)rhs * 3 * F.S;
-  C_t<T>* fc = Cc.f + (long)rhs * 3 * Cc.S;
-  C_t<T>* uc = Cc.u + (long)rhs * 3 * Cc.S;
+  const int c = blockIdx.z;  // one component per thread
+  C_t<T>* fc = Cc.f + ((long)rhs * 3 + c) * Cc.S;
+  C_t<T>* uc = Cc.u + ((long)rhs * 3 + c) * Cc.S;
   const Geo<T> Gf{F.geo + (long)op_of(F, rhs) * F.gstride, F.gmax1};
   const Geo<T> Gc{Cc.geo + (long)op_of(Cc, rhs) * Cc.gstride, Cc.gmax1};
-  fc[s] = restrict_comp<T, 0>(F, Cc, sc, Cn, rf, Gf, Gc);
-  fc[Cc.S + s] = restrict_comp<T, 1>(F, Cc, sc, Cn, rf, Gf, Gc);
-  fc[2 * Cc.S + s] = restrict_comp<T, 2>(F, Cc, sc, Cn, rf, Gf, Gc);
+  C_t<T> v;
+  switch (c) {
+    case 0: v = restrict_comp<T, 0>(F, Cc, sc, Cn, rf, Gf, Gc); break;
+    case 1: v = restrict_comp<T, 1>(F, Cc, sc, Cn, rf, Gf, Gc); break;
+    default: v = restrict_comp<T, 2>(F, Cc, sc, Cn, rf, Gf, Gc); break;
+  }
+  fc[s] = v;
   uc[s] = mk<T>(0, 0);
-  uc[Cc.S + s] = mk<T>(0, 0);
-  uc[2 * Cc.S + s] = mk<T>(0, 0);
 }
 
 template <typename T>
 void launch_restrict(const LevelView<T>& F, const LevelView<T>& Cc, const int sc[3], cudaStream_t st) {
-  dim3 grid((unsigned)((Cc.S + 255) / 256), Cc.nrhs);
+  dim3 grid((unsigned)((Cc.S + 255) / 256), Cc.nrhs, 3);
   k_restrict<T><<<grid, 256, 0, st>>>(F, Cc, sc[0], sc[1], sc[2]);
 }
 
@@ -1482,20 +1485,17 @@ __device__ __forceinline__ void prolong_comp(const LevelView<T>& F, const LevelV
   const T wr1 = (xf1[P[t1]] - xc1[Cn[t1]]) / (xc1[Cn[t1] + 1] - xc1[Cn[t1]]);
   const T wr2 = (xf2[P[t2]] - xc2[Cn[t2]]) / (xc2[Cn[t2] + 1] - xc2[Cn[t2]]);
   const T wl1 = T(1) - wr1, wl2 = T(1) - wr2;
-  int Q[3] = {Cn[0], Cn[1], Cn[2]};
-  const long b = (long)C * Cc.S;
-  const C_t<T> u00 = uc[b + slot_id(Cc.n, Q[0], Q[1], Q[2])];
-  Q[t2] += 1;
-  const C_t<T> u01 = uc[b + slot_id(Cc.n, Q[0], Q[1], Q[2])];
-  Q[t2] -= 1;
-  Q[t1] += 1;
-  const C_t<T> u10 = uc[b + slot_id(Cc.n, Q[0], Q[1], Q[2])];
-  Q[t2] += 1;
-  const C_t<T> u11 = uc[b + slot_id(Cc.n, Q[0], Q[1], Q[2])];
-  C_t<T> v = uf[(long)C * F.S + s];
+  // 32-bit offsets: the four coarse neighbours differ by the strides of t1, t2
+  const int cs[3] = {1, Cc.n[0] + 1, (Cc.n[0] + 1) * (Cc.n[1] + 1)};
+  const int q00 = C * (int)Cc.S + slot_id32(Cc.n, Cn[0], Cn[1], Cn[2]);
+  const C_t<T> u00 = uc[q00];
+  const C_t<T> u01 = uc[q00 + cs[t2]];
+  const C_t<T> u10 = uc[q00 + cs[t1]];
+  const C_t<T> u11 = uc[q00 + cs[t1] + cs[t2]];
+  C_t<T> v = uf[C * (int)F.S + (int)s];
   v.x += wl1 * (wl2 * u00.x + wr2 * u01.x) + wr1 * (wl2 * u10.x + wr2 * u11.x);
   v.y += wl1 * (wl2 * u00.y + wr2 * u01.y) + wr1 * (wl2 * u10.y + wr2 * u11.y);
-  uf[(long)C * F.S + s] = v;
+  uf[C * (int)F.S + (int)s] = v;
 }
 
 template <typename T>
@@ -1508,19 +1508,21 @@ __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> Cc
   const int sc[3] = {sc0, sc1, sc2};
   const int n0 = F.n[0] + 1, n1 = F.n[1] + 1;
   int P[3];
-    slot_nodes(s, n0, n1, P);
+  slot_nodes(s, n0, n1, P);
   C_t<T>* uf = F.u + (long)rhs * 3 * F.S;
   const C_t<T>* uc = Cc.u + (long)rhs * 3 * Cc.S;
   const Geo<T> Gf{F.geo + (long)op_of(F, rhs) * F.gstride, F.gmax1};
   const Geo<T> Gc{Cc.geo + (long)op_of(Cc, rhs) * Cc.gstride, Cc.gmax1};
-  prolong_comp<T, 0>(F, Cc, sc, P, uf, uc, Gf, Gc, s);
-  prolong_comp<T, 1>(F, Cc, sc, P, uf, uc, Gf, Gc, s);
-  prolong_comp<T, 2>(F, Cc, sc, P, uf, uc, Gf, Gc, s);
+  switch (blockIdx.z) {  // one component per thread
+    case 0: prolong_comp<T, 0>(F, Cc, sc, P, uf, uc, Gf, Gc, s); break;
+    case 1: prolong_comp<T, 1>(F, Cc, sc, P, uf, uc, Gf, Gc, s); break;
+    default: prolong_comp<T, 2>(F, Cc, sc, P, uf, uc, Gf, Gc, s); break;
+  }
 }
 
 template <typename T>
 void launch_prolong(const LevelView<T>& F, const LevelView<T>& Cc, const int sc[3], cudaStream_t st) {
-  dim3 grid((unsigned)((F.S + 255) / 256), F.nrhs);
+  dim3 grid((unsigned)((F.S + 255) / 256), F.nrhs, 3);
   k_prolong<T><<<grid, 256, 0, st>>>(F, Cc, sc[0], sc[1], sc[2]);
 }
 
