@@ -52,6 +52,26 @@ template <typename T> __device__ __forceinline__ C_t<T> crcp(C_t<T> z) {
 // launch; lets loads move past the kernel's own stores
 template <typename T> __device__ __forceinline__ T ldro(const T* p) { return __ldg(p); }
 
+// Division by a divisor fixed for a launch, for dividends below 2^31, as a
+// multiply-high, an add and a shift: with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, u / d = (umulhi(u, m) + u) >> l
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994).  Constants come from the host.
+struct FastDiv {
+  unsigned m, l;
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  unsigned l = 0;
+  while ((1ull << l) < d) l++;
+  FastDiv f;
+  f.l = l;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned u, const FastDiv& f) {
+  return (__umulhi(u, f.m) + u) >> f.l;
+}
+
 // ---------------------------------------------------------------- views
 // One multigrid level of a batch, in working precision T.
 template <typename T> struct LevelView {
@@ -69,7 +89,14 @@ template <typename T> struct LevelView {
   const T* wmu;      // [nrhs] omega*mu0 (the operator's mass term is -i wmu sigma)
   const int* active; // [nrhs] nonzero = work on this RHS (may be null)
   const int* op;     // [nrhs] operator (geo/cells) index of each RHS (null: identity)
+  FastDiv d0, d1;    // division by n[0]+1 and n[1]+1 (set_slot_divs)
 };
+
+// the slot-decode divisors of a view, set on the host wherever a view is built
+template <typename T> inline void set_slot_divs(LevelView<T>& V) {
+  V.d0 = make_fastdiv((unsigned)(V.n[0] + 1));
+  V.d1 = make_fastdiv((unsigned)(V.n[1] + 1));
+}
 
 template <typename T> __device__ __forceinline__ int op_of(const LevelView<T>& L, int rhs) {
   return L.op ? L.op[rhs] : rhs;
@@ -201,26 +228,6 @@ __device__ __forceinline__ int nbr_delta32(int k, const int ss[3], int S) {
   return o.comp * S + o.dc * ss[C] + o.dp * ss[p] + o.dq * ss[q];
 }
 
-// Division by a divisor fixed for a launch, for dividends below 2^31, as a
-// multiply-high, an add and a shift: with l = ceil(log2 d) and
-// m = floor(2^32 (2^l - d) / d) + 1, u / d = (umulhi(u, m) + u) >> l
-// (Granlund and Montgomery, "Division by invariant integers using
-// multiplication", PLDI 1994).  Constants come from the host.
-struct FastDiv {
-  unsigned m, l;
-};
-inline FastDiv make_fastdiv(unsigned d) {
-  unsigned l = 0;
-  while ((1ull << l) < d) l++;
-  FastDiv f;
-  f.l = l;
-  f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
-  return f;
-}
-__device__ __forceinline__ unsigned fdiv(unsigned u, const FastDiv& f) {
-  return (__umulhi(u, f.m) + u) >> f.l;
-}
-
 // slot index -> node indices with 32-bit arithmetic (a level holds fewer
 // than 2^31 slots per right-hand side): one division and one modulo fewer
 // than the 64-bit decomposition, which dominated the index work
@@ -230,6 +237,16 @@ __device__ __forceinline__ void slot_nodes(long s, int n0, int n1, int P[3]) {
   P[0] = (int)(u - t * a);
   P[1] = (int)(t % b);
   P[2] = (int)(t / b);
+}
+// the same with the view's launch-invariant divisors (multiply-high)
+template <typename T>
+__device__ __forceinline__ void slot_nodes(long s, const LevelView<T>& L, int P[3]) {
+  const unsigned u = (unsigned)s, a = (unsigned)(L.n[0] + 1), b = (unsigned)(L.n[1] + 1);
+  const unsigned t = fdiv(u, L.d0);
+  const unsigned k = fdiv(t, L.d1);
+  P[0] = (int)(u - t * a);
+  P[1] = (int)(t - k * b);
+  P[2] = (int)k;
 }
 
 // (A u) of the edge equation of component C at slot s, and its coefficients

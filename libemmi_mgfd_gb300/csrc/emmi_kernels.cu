@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
   if (s < L.S) {
     const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
     int P[3];
-    slot_nodes(s, n0, n1, P);
+    slot_nodes(s, L, P);
     const long ss[3] = {1, (long)n0, (long)n0 * n1};
     const C_t<T>* u = L.u + (long)rhs * 3 * L.S;
     const C_t<T>* f = L.f ? L.f + (long)rhs * 3 * L.S : nullptr;
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(256) k_coef64(LevelView<double> L, double* __r
   if (s >= L.S) return;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   int P[3];
-  slot_nodes(s, n0, n1, P);
+  slot_nodes(s, L, P);
   const double* cells = L.cells + (long)op * 4 * L.ncell;
   const Geo<double> G{L.geo + (long)op * L.gstride, L.gmax1};
   double* out = coef + (long)op * kCoef * 3 * L.S;
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(256) k_residual_coef(LevelView<double> L,
   if (s < L.S) {
     const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
     int P[3];
-    slot_nodes(s, n0, n1, P);
+    slot_nodes(s, L, P);
     const long ss[3] = {1, (long)n0, (long)n0 * n1};
     const double2* u = L.u + (long)rhs * 3 * L.S;
     const double2* f = L.f ? L.f + (long)rhs * 3 * L.S : nullptr;
@@ -1442,9 +1442,8 @@ __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= Cc.S) return;
   const int sc[3] = {sc0, sc1, sc2};
-  const int n0 = Cc.n[0] + 1, n1 = Cc.n[1] + 1;
   int Cn[3];
-  slot_nodes(s, n0, n1, Cn);
+  slot_nodes(s, Cc, Cn);
   const C_t<T>* rf = F.r + (long)rhs * 3 * F.S;
   const int c = blockIdx.z;  // one component per thread
   C_t<T>* fc = Cc.f + ((long)rhs * 3 + c) * Cc.S;
@@ -1506,9 +1505,8 @@ __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> Cc
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= F.S) return;
   const int sc[3] = {sc0, sc1, sc2};
-  const int n0 = F.n[0] + 1, n1 = F.n[1] + 1;
   int P[3];
-  slot_nodes(s, n0, n1, P);
+  slot_nodes(s, F, P);
   C_t<T>* uf = F.u + (long)rhs * 3 * F.S;
   const C_t<T>* uc = Cc.u + (long)rhs * 3 * Cc.S;
   const Geo<T> Gf{F.geo + (long)op_of(F, rhs) * F.gstride, F.gmax1};

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256) k_ls_input(LevelView<float> L, const floa
   if (s >= L.S) return;
   const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   int P[3];
-  slot_nodes(s, n0, n1, P);
+  slot_nodes(s, L, P);
   const long ss[3] = {1, (long)n0, (long)n0 * n1};
   const float2* u = L.u + (long)b * 3 * L.S;
   const float2* f = L.f ? L.f + (long)b * 3 * L.S : nullptr;

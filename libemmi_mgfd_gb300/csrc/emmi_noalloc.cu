@@ -129,6 +129,7 @@ int sweep_noalloc(const int n[3], const double* const xin[3], const void* cells,
 
   LevelView<T> V;
   for (int k = 0; k < 3; k++) V.n[k] = n[k];
+  set_slot_divs(V);
   V.nrhs = 1;
   V.S = (long)(n[0] + 1) * (n[1] + 1) * (n[2] + 1);
   V.ncell = (long)n[0] * n[1] * n[2];

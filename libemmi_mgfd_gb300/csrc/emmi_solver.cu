@@ -266,6 +266,7 @@ LevelView<double> emmi_solver::view<double>(int h, int l) const {
   V.wmu = d_wmu64;
   V.active = d_active;
   V.op = d_op;
+  set_slot_divs(V);
   return V;
 }
 
@@ -287,6 +288,7 @@ LevelView<float> emmi_solver::view<float>(int h, int l) const {
   V.wmu = d_wmu32;
   V.active = d_active;
   V.op = d_op;
+  set_slot_divs(V);
   return V;
 }
 
@@ -1342,6 +1344,7 @@ int level_op(const int n[3], const double* x1, const double* x2, const double* x
   }
   LevelView<T> V;
   for (int e = 0; e < 3; e++) V.n[e] = n[e];
+  set_slot_divs(V);
   V.nrhs = 1;
   V.S = S;
   V.ncell = nc;
