@@ -64,6 +64,9 @@ def parse():
                         "range emmi_profile (for ncu --nvtx-include emmi_profile/)")
     p.add_argument("--profile-dir", type=int, default=0, choices=(0, 1, 2),
                    help="with --profile: the line direction of the sweep (0 x, 1 y, 2 z)")
+    p.add_argument("--profile-residual", action="store_true",
+                   help="with --profile: one complex64 residual r = f - A u of a seeded 128^3 "
+                        "level (unit spacing, random conductivity), one RHS")
     p.add_argument("--profile-learned", action="store_true",
                    help="with --profile: one application of the learned correction (seeded "
                         "weights, seeded level-0 iterates) instead of the line sweep")
@@ -262,7 +265,20 @@ def main():
     if a.profile:
         sp = make_solver(w, G.PREC_MIXED, a.tol)
         sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
-        if a.profile_learned:
+        if a.profile_residual:
+            rng = np.random.default_rng(12)
+            n3 = (a.n, a.n, a.n)
+            xs = [np.arange(v + 1, dtype=np.float64) for v in n3]
+            cells = np.concatenate([10.0 ** rng.uniform(-2, 0, (3, a.n ** 3)),
+                                    np.ones((1, a.n ** 3))])
+            S3 = 3 * (a.n + 1) ** 3
+            u = rng.standard_normal(S3) + 1j * rng.standard_normal(S3)
+            f = rng.standard_normal(S3) + 1j * rng.standard_normal(S3)
+            G.level_residual(n3, xs, cells, 6.28, u, f, prec=G.PREC_MIXED)  # warm-up
+            torch.cuda.nvtx.range_push("emmi_profile")
+            G.level_residual(n3, xs, cells, 6.28, u, f, prec=G.PREC_MIXED)
+            torch.cuda.nvtx.range_pop()
+        elif a.profile_learned:
             rng = np.random.default_rng(11)
             sp.set_learned((0.05 * rng.standard_normal(2 * 27 * 64)).astype(np.float32))
             shape = (nrhs, 3 * sp.nslots)

@@ -85,6 +85,20 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+// a thread's partial sum of squares in working precision: complex64
+// residuals square and add across the warp in fp32 and widen once per warp
+// (conversions to FP64 and FP64 arithmetic are low-rate on this GPU); the
+// block and the grid sum in FP64
+template <typename T>
+__device__ __forceinline__ double warp_partial(T v) {
+  if constexpr (sizeof(T) == 4) return (double)warp_sum(v);
+  else return warp_sum((double)v);
+}
 
 __device__ __forceinline__ void block_add(double v, double* dst) {
   __shared__ double red[32];
@@ -100,6 +114,22 @@ __device__ __forceinline__ void block_add(double v, double* dst) {
   }
 }
 
+// block_add for a thread's partial of type T (see warp_partial)
+template <typename T>
+__device__ __forceinline__ void block_add_t(T v, double* dst) {
+  __shared__ double red[32];
+  double w = warp_partial<T>(v);
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  if (lane == 0) red[wi] = w;
+  __syncthreads();
+  if (wi == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    w = lane < nw ? red[lane] : 0.0;
+    w = warp_sum(w);
+    if (lane == 0 && w != 0.0) atomicAdd(dst, w);
+  }
+}
+
 // ------------------------------------------------------------ residual
 template <int C>
 __device__ __forceinline__ bool is_unknown(const int n[3], const int P[3]) {
@@ -108,7 +138,7 @@ __device__ __forceinline__ bool is_unknown(const int n[3], const int P[3]) {
 }
 
 template <typename T, typename TO, int C>
-__device__ __forceinline__ double residual_comp(const LevelView<T>& L, const C_t<T>* u,
+__device__ __forceinline__ T residual_comp(const LevelView<T>& L, const C_t<T>* u,
                                                 const C_t<T>* f, const T* cells, const Geo<T>& G,
                                                 T wmu, const int P[3], long s, const long ss[3],
                                                 C_t<TO>* rout) {
@@ -120,7 +150,7 @@ __device__ __forceinline__ double residual_comp(const LevelView<T>& L, const C_t
     r = csub<T>(r, au);
   }
   if (rout) rout[o] = mk<TO>((TO)r.x, (TO)r.y);
-  return (double)r.x * (double)r.x + (double)r.y * (double)r.y;
+  return r.x * r.x + r.y * r.y;
 }
 
 // a thread per (component, slot), the component = blockIdx.z: one edge
@@ -131,7 +161,7 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
   const int rhs = blockIdx.y;
   if (L.active && !L.active[rhs]) return;
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  double acc = 0.0;
+  T acc = 0;
   if (s < L.S) {
     const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
     int P[3];
@@ -149,7 +179,7 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
       default: acc = residual_comp<T, TO, 2>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
     }
   }
-  if (norm2) block_add(acc, norm2 + rhs);
+  if (norm2) block_add_t<T>(acc, norm2 + rhs);
 }
 
 template <typename T, typename TO>
