@@ -114,6 +114,10 @@ double emmi_solver_last_time(const emmi_solver *s);
 long emmi_solver_last_launches(const emmi_solver *s);
 /* Device bytes held by the solver. */
 size_t emmi_solver_device_bytes(const emmi_solver *s);
+/* The stored line factors of a MIXED solver: 1 = L in fp16 with 1/d in
+ * fp32, 0 = fp32 (asked for, or after an L value left the fp16 range),
+ * -1 = none (factoring in every sweep).  No counterpart in the reference. */
+int emmi_solver_line_factor_format(const emmi_solver *s);
 /* The CUDA stream (cudaStream_t) every launch of this solver goes to. */
 void *emmi_solver_stream(const emmi_solver *s);
 /* Time `reps` full level-0 line-relaxation sweeps (4 colours, all RHS) along

@@ -1286,6 +1286,9 @@ int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int
 double emmi_solver_last_time(const emmi_solver* s) { return s ? s->last_time : 0.0; }
 long emmi_solver_last_launches(const emmi_solver* s) { return s ? s->last_launches : 0; }
 size_t emmi_solver_device_bytes(const emmi_solver* s) { return s ? s->bytes : 0; }
+int emmi_solver_line_factor_format(const emmi_solver* s) {
+  return s && s->fac_on ? s->fac_fmt : -1;
+}
 
 void emmi_solver_destroy(emmi_solver* s) {
   if (!s) return;

@@ -306,6 +306,11 @@ class Solver:
     def device_bytes(self) -> int:
         return lib().emmi_solver_device_bytes(self._h)
 
+    @property
+    def line_factor_format(self) -> int:
+        """1: stored factors with L in fp16; 0: fp32; -1: none."""
+        return lib().emmi_solver_line_factor_format(self._h)
+
     def close(self):
         if getattr(self, "_h", None):
             lib().emmi_solver_destroy(self._h)

@@ -247,3 +247,28 @@ def test_fp16_line_factors_converge_like_fp32(golden):
         assert abs(c2 - c1) <= max(2, c1 // 10), (c2, c1)
         assert rel_err(out[2][0][r], out[1][0][r], sea) < 1e-6
         assert rel_err(out[2][1][r], out[1][1][r]) < 1e-6
+
+
+@gpu
+def test_fp16_factor_overflow_falls_back_to_fp32():
+    """Cells 10^6 times thinner along x than along y and z make the x-line
+    factors' L values exceed the fp16 range: set-up detects it and keeps fp32
+    factors (a normal grid keeps fp16); the solve runs on them."""
+    G = _G()
+    n = (8, 8, 8)
+    rng = np.random.default_rng(3)
+    raw = np.concatenate([10.0 ** rng.uniform(-2, 0, (3, 8, 8, 8)),
+                          np.ones((1, 8, 8, 8))]).astype(np.float32)
+    b = np.zeros((1, 3 * 9 ** 3), np.complex128)
+    b[0, 3 * 9 ** 3 // 2] = 1.0
+    fmts = {}
+    for name, dx in (("normal", 100.0), ("thin", 1e-4)):
+        x = [np.arange(9, dtype=np.float32) * dx, np.arange(9, dtype=np.float32) * 100.0,
+             np.arange(9, dtype=np.float32) * 100.0]
+        s = G.Solver(n, *x, raw[None], np.array([6.28], np.float32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=3, tol=0.0))
+        fmts[name] = s.line_factor_format
+        xs, hs, st = s.solve(b)
+        assert np.all(np.isfinite(xs)), name
+        s.close()
+    assert fmts == {"normal": 1, "thin": 0}, fmts
