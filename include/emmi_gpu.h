@@ -129,6 +129,10 @@ void *emmi_solver_stream(const emmi_solver *s);
 int emmi_solver_time_smoother(emmi_solver *s, int dir, int reps, double *ms,
                               int *launches, double *bytes);
 void emmi_solver_destroy(emmi_solver *s);
+/* Solver memory comes from the device's stream-ordered memory pool and goes
+ * back to it on destroy, where it stays for the next solver; this returns
+ * the pool's unused memory to the device.  No counterpart in the reference. */
+int emmi_trim_memory(void);
 
 const char *emmi_last_error(void);
 

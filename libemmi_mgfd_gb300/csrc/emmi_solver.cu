@@ -20,6 +20,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <mutex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -224,9 +227,41 @@ inline unsigned blocks_for(long n, int bs = 256, long cap = 65535) {
 }  // namespace
 
 
+// Solver memory comes from the device's stream-ordered pool on the solver's
+// stream; freed memory stays in the pool (release threshold raised once per
+// device) so that destroying and creating solvers does not map and unmap
+// device memory each time.  emmi_trim_memory gives it back.
+static void keep_pool_memory() {
+  static std::once_flag once[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  std::call_once(once[dev], [dev] {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return;
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  });
+}
+
+// device memory a new allocation can have: free memory plus what the pool
+// holds unused
+static size_t device_avail() {
+  size_t freeb = 0, totb = 0;
+  if (cudaMemGetInfo(&freeb, &totb) != cudaSuccess) return 0;
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t res = 0, used = 0;
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &res);
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    if (res > used) freeb += (size_t)(res - used);
+  }
+  return freeb;
+}
+
 int emmi_solver::alloc(void** p, size_t b) {
   if (b == 0) b = 16;
-  cudaError_t e = cudaMalloc(p, b);
+  cudaError_t e = cudaMallocAsync(p, b, st);
   if (e != cudaSuccess) {
     set_err("cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
     return EMMI_ENOMEM;
@@ -240,7 +275,7 @@ int emmi_solver::alloc(void** p, size_t b) {
 void emmi_solver::release(void* p) {
   for (size_t i = 0; i < allocs.size(); i++)
     if (allocs[i] == p) {
-      cudaFree(p);
+      cudaFreeAsync(p, st);
       bytes -= alloc_bytes[i];
       allocs.erase(allocs.begin() + i);
       alloc_bytes.erase(alloc_bytes.begin() + i);
@@ -489,8 +524,7 @@ static int build_line_factors(emmi_solver* s) {
           }
         }
     if (total == 0) return EMMI_OK;
-    size_t freeb = 0, totb = 0;
-    CK(cudaMemGetInfo(&freeb, &totb));
+    const size_t freeb = device_avail();
     const size_t bytes = (size_t)total * sizeof(float);
     if (bytes > freeb / 2) return EMMI_OK;  // factor in every sweep instead
     if ((rc = s->alloc((void**)&s->d_fac, bytes)) != EMMI_OK) return rc;
@@ -562,9 +596,7 @@ static int build_line_factors(emmi_solver* s) {
 static int build_coef64(emmi_solver* s) {
   const HLev& L0 = s->hier[0][0];
   const size_t bytes = (size_t)s->nop * coef64_elems(L0.n) * sizeof(double);
-  size_t freeb = 0, totb = 0;
-  CK(cudaMemGetInfo(&freeb, &totb));
-  if (bytes > freeb / 2) return EMMI_OK;
+  if (bytes > device_avail() / 2) return EMMI_OK;
   int rc;
   if ((rc = s->alloc((void**)&s->d_coef64, bytes)) != EMMI_OK) return rc;
   CK(cudaMemsetAsync(s->d_coef64, 0, bytes, s->st));
@@ -572,9 +604,17 @@ static int build_coef64(emmi_solver* s) {
   V.nrhs = s->nop;
   V.op = nullptr;
   V.active = nullptr;
-  launch_coef64(V, s->d_coef64, s->st);
+  // FP64-bound work that no step needs before the first refinement: on a
+  // side stream, overlapping the first complex64 cycles (true_residual64
+  // waits for ev_coef)
+  CK(cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&s->ev_coef, cudaEventDisableTiming));
+  CK(cudaEventRecord(s->ev_coef, s->st));
+  CK(cudaStreamWaitEvent(s->st2, s->ev_coef, 0));
+  launch_coef64(V, s->d_coef64, s->st2);
   CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(s->st));
+  CK(cudaEventRecord(s->ev_coef, s->st2));
+  s->coef_pending = true;
   return EMMI_OK;
 }
 
@@ -663,7 +703,18 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
       return EMMI_ECUDA;                                                         \
     }                                                                            \
   } while (0)
+  // set-up phase times on stderr with verb >= 2 (each mark drains the stream)
+  auto t_last = std::chrono::steady_clock::now();
+  auto mark = [&](const char* what) {
+    if (s->opt.verb < 2) return;
+    cudaStreamSynchronize(s->st);
+    const auto now = std::chrono::steady_clock::now();
+    fprintf(stderr, "emmi_solver_create: %-28s %8.2f ms\n", what,
+            std::chrono::duration<double, std::milli>(now - t_last).count());
+    t_last = now;
+  };
   init_line_kernels();
+  keep_pool_memory();
   CKS(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
   CKS(cudaEventCreate(&s->ev0));
   CKS(cudaEventCreate(&s->ev1));
@@ -857,6 +908,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     CKS(cudaGetLastError());
     CKS(cudaStreamSynchronize(s->st));
   }
+  mark("geometry and cells");
 
   // ---- fields: level 0 per mode, coarse levels sized by the largest hierarchy
   {
@@ -891,8 +943,11 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     s->scratch_bytes = std::max<size_t>((size_t)per_rhs * esz * s->chunk, 16);
     TRY(s->alloc(&s->scratch, s->scratch_bytes));
     if (mixed && s->opt.krylov > 0) TRY(krylov_alloc(s));
+    mark("field buffers");
     if (mixed && s->opt.line_factors) TRY(build_line_factors(s));
+    mark("line factors");
     if (mixed) TRY(build_coef64(s));
+    mark("FP64 coefficients");
   }
 
   // ---- graphs
@@ -903,6 +958,7 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
       return rc;
     }
   }
+  mark("CUDA graphs");
   *out = s;
   return EMMI_OK;
 #undef TRY
@@ -1292,16 +1348,36 @@ int emmi_solver_line_factor_format(const emmi_solver* s) {
 
 void emmi_solver_destroy(emmi_solver* s) {
   if (!s) return;
+  if (s->st2) {
+    cudaStreamSynchronize(s->st2);
+    cudaStreamDestroy(s->st2);
+  }
+  if (s->ev_coef) cudaEventDestroy(s->ev_coef);
   if (s->st) cudaStreamSynchronize(s->st);
   for (int h = 0; h < 3; h++) {
     if (s->gA[h]) cudaGraphExecDestroy(s->gA[h]);
     if (s->gB[h]) cudaGraphExecDestroy(s->gB[h]);
   }
-  for (void* p : s->allocs) cudaFree(p);
+  if (s->st) {
+    for (void* p : s->allocs) cudaFreeAsync(p, s->st);
+    cudaStreamSynchronize(s->st);
+  }
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
+}
+
+int emmi_trim_memory(void) {
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) {
+    set_err("emmi_trim_memory: no device memory pool");
+    return EMMI_ECUDA;
+  }
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemPoolTrimTo(pool, 0));
+  return EMMI_OK;
 }
 
 }  // extern "C"

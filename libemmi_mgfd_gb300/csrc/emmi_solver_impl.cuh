@@ -63,6 +63,11 @@ struct emmi_solver {
 
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // side stream of the set-up work no step needs at once (the stored FP64
+  // coefficients), and the event the first use waits for
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_coef = nullptr;
+  bool coef_pending = false;
   cudaGraphExec_t gA[3] = {}, gB[3] = {};
   long nodesA[3] = {}, nodesB[3] = {};
   double last_time = 0;
@@ -140,6 +145,10 @@ int run_part(emmi_solver* s, int h, int part);
 template <typename TO>
 inline void true_residual64(emmi_solver* s, const emmi::LevelView<double>& V, emmi::C_t<TO>* rout,
                             double* norm2) {
+  if (s->coef_pending) {  // the coefficients come from the side stream
+    cudaStreamWaitEvent(s->st, s->ev_coef, 0);
+    s->coef_pending = false;
+  }
   if (s->d_coef64)
     emmi::launch_residual_coef<TO>(V, s->d_coef64, rout, norm2, s->st);
   else

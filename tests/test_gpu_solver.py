@@ -272,3 +272,19 @@ def test_fp16_factor_overflow_falls_back_to_fp32():
         assert np.all(np.isfinite(xs)), name
         s.close()
     assert fmts == {"normal": 1, "thin": 0}, fmts
+
+
+@gpu
+def test_pooled_memory_is_reused_and_trimmed(golden):
+    """Solver memory comes from the device's stream-ordered pool: a second
+    solver of the same size reuses what the first gave back, and
+    emmi_trim_memory returns the pool's unused memory to the device."""
+    import torch
+    G = _G()
+    g = golden("tiny_layered")
+    for _ in range(2):
+        s = _solver(g, ncycle=2, tol=0.0)
+        s.solve(g["b_f0"][None])
+        s.close()
+    assert G.lib().emmi_trim_memory() == 0
+    torch.cuda.synchronize()
