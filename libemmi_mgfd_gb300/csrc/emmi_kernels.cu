@@ -449,7 +449,8 @@ __device__ __forceinline__ bool line_item_fd(const LineGeom& g, const LineDiv& v
   return true;
 }
 
-template <typename T, int D, int TT, int C>
+// RES false: the band entries only (factor set-up; the residual slot is 0)
+template <typename T, int D, int TT, int C, bool RES = true>
 __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>* u,
                                              const C_t<T>* f, const T* cells, const Geo<T>& G,
                                              T wmu, int ta, int tb, int s, int row,
@@ -462,8 +463,13 @@ __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>
   P[B] = tb - (TT == 3 ? 1 : 0);
   const int sl = P[0] + (L.n[0] + 1) * (P[1] + (L.n[1] + 1) * P[2]);  // 32-bit slot
   EdgeCoef<T> e;
-  const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
-  const C_t<T> r = csub<T>(f[C * (int)L.S + sl], au);
+  C_t<T> r = mk<T>(0, 0);
+  if constexpr (RES) {
+    const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
+    r = csub<T>(f[C * (int)L.S + sl], au);
+  } else {
+    edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
+  }
   T band[5] = {0, 0, 0, 0, 0};
 #define LINE_ENTRY(K)                                                         \
   {                                                                           \
@@ -498,8 +504,8 @@ __device__ __forceinline__ long line_slot(const int n[3], long S, int ta, int tb
 }
 
 // one thread per (line, node) and its five rows: y and z lines, whose
-// neighbouring lines are neighbouring slots
-template <typename T, int D>
+// neighbouring lines are neighbouring slots (RES false: band entries only)
+template <typename T, int D, bool RES = true>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(LevelView<T> L,
                                                                               int pa, int pb,
                                                                               T* __restrict__ buf) {
@@ -524,12 +530,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(L
   const long ps = g.nl;
   const int r0 = 5 * (s - 1);
   auto rec = [&](int row) { return base + (long)row * kPlanes<T> * g.nl + l; };
-  assemble_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0), ps);
+  assemble_row<T, D, 0, D, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0), ps);
   if (s < g.nd) {
-    assemble_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1), ps);
-    assemble_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2), ps);
-    assemble_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3), ps);
-    assemble_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4), ps);
+    assemble_row<T, D, 1, A, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1), ps);
+    assemble_row<T, D, 2, A, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2), ps);
+    assemble_row<T, D, 3, B, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3), ps);
+    assemble_row<T, D, 4, B, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4), ps);
   }
 }
 
@@ -1185,7 +1191,7 @@ static void line_factor_d(const LevelView<T>& L, int color, T* buf, T* fac, int 
   const int m = 5 * L.n[D] - 4;
   const long gstride = line_factor_elems(L.n, D, color, fmt);
   dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
-  k_line_assemble<T, D><<<g1, 256, 0, st>>>(L, pa, pb, buf);
+  k_line_assemble<T, D, false><<<g1, 256, 0, st>>>(L, pa, pb, buf);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
   if constexpr (std::is_same<T, float>::value) {
     if (fmt == kFacF16) {
