@@ -129,6 +129,25 @@ void *emmi_solver_stream(const emmi_solver *s);
 int emmi_solver_time_smoother(emmi_solver *s, int dir, int reps, double *ms,
                               int *launches, double *bytes);
 void emmi_solver_destroy(emmi_solver *s);
+/* emmi_solver_create with P->cells in device memory (the rest of P on the
+ * host), e.g. from emmi_homogenize_batch: no host round trip of the cells.
+ * No counterpart in the reference. */
+int emmi_solver_create_dc(emmi_solver **out, const emmi_problem *P,
+                          const emmi_options *opts);
+/* The homogenization of the reference's regrid stage on the device for
+ * nshots shots over one model (src/homogenization.c:15-111,
+ * src/regrid_init_free.c:206-226): the padded model pad[3][nzp][nyp][nxp]
+ * (sigma11, sigma22, rho33) on the node axes xx, yy, zz (eh_pad_model of
+ * the host library) averaged onto each shot's cells x1[nshots][n1+1], x2,
+ * x3 (eh_regrid_axes), written as cells[nshots][4][n3][n2][n1] (sigma11,
+ * sigma22, sigma33 = 1 / rho33 average, invmur = 1) in device memory; every
+ * other pointer is host memory.  Bit for bit the host front end's
+ * (eh_regrid).  Synchronises the stream. */
+int emmi_homogenize_batch(int nxp, int nyp, int nzp, const float *xx,
+                          const float *yy, const float *zz, const float *pad,
+                          int nshots, int n1, int n2, int n3, const float *x1,
+                          const float *x2, const float *x3, float *cells,
+                          void *stream);
 /* Solver memory comes from the device's stream-ordered memory pool and goes
  * back to it on destroy, where it stays for the next solver; this returns
  * the pool's unused memory to the device.  No counterpart in the reference. */

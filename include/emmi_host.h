@@ -60,6 +60,20 @@ int eh_homogenize(const float *in, float *out, int nx, int ny, int nz,
  * out arrays preallocated by the caller. */
 int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *out);
 
+/* The two halves of eh_regrid, for a batch of shots over one model:
+ * eh_pad_dims gives the padded model's cells (nx + 2 nb, ...);
+ * eh_pad_model the padded node axes xx[nxp+1], yy[nyp+1], zz[nzp+1] and the
+ * padded model pad[3][nzp][nyp][nxp] (sigma11, sigma22, rho33) once per
+ * model (regrid_init_free.c:47-141); eh_regrid_axes the shot's mesh axes
+ * and their staggered copies in g (regrid_init_free.c:156-214; the
+ * conductivity arrays of g are not touched).  Homogenizing pad onto the
+ * axes (eh_homogenize, or the GPU library's emmi_homogenize_batch) gives
+ * eh_regrid's conductivities. */
+int eh_pad_dims(const eh_model *m, int *nxp, int *nyp, int *nzp);
+int eh_pad_model(const eh_model *m, float *xx, float *yy, float *zz, float *pad);
+int eh_regrid_axes(const eh_model *m, const float *xx, const float *yy,
+                   const float *zz, float sx, float sy, float sz, eh_grid *g);
+
 /* emf_init_free.c:114-128: the smallest resistivity of the three cubes */
 float eh_rho_water(const eh_model *m);
 

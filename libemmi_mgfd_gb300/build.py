@@ -21,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 GPU_SOURCES = ["emmi_kernels.cu", "emmi_solver.cu", "emmi_survey.cu", "emmi_dropin.cu",
-               "emmi_krylov.cu", "emmi_learned.cu", "emmi_noalloc.cu"]
+               "emmi_krylov.cu", "emmi_learned.cu", "emmi_noalloc.cu", "emmi_frontend.cu"]
 HOST_SOURCES = ["emmi_host.c"]
 GPU_LIB = os.path.join(HERE, "libemmi_gpu.so")
 HOST_LIB = os.path.join(HERE, "libemmi_host.so")

@@ -155,25 +155,26 @@ static void centred_axis(int n, float src, float lo, float hi, float dmin, float
   free(x);
 }
 
-int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *g) {
-  if (!m || !g || m->nx < 1 || m->ny < 1 || m->nz < 1 || m->nb < 0 || m->n1 < 2 || m->n2 < 2 ||
-      m->n3 < 2)
-    return EH_EINVAL;
+int eh_pad_dims(const eh_model *m, int *nxp, int *nyp, int *nzp) {
+  if (!m || m->nx < 1 || m->ny < 1 || m->nz < 1 || m->nb < 0) return EH_EINVAL;
+  *nxp = m->nx + 2 * m->nb;
+  *nyp = m->ny + 2 * m->nb;
+  *nzp = m->nz + 2 * m->nb;
+  return EH_OK;
+}
+
+/* padded model: interior copied (sigma = 1/rho for 11/22, rho for 33),
+ * edges replicated, nb air cells on top (regrid_init_free.c:82-141); the
+ * padded node axes (regrid_init_free.c:47-70) */
+int eh_pad_model(const eh_model *m, float *xx, float *yy, float *zz, float *pad) {
+  int nxp, nyp, nzp;
+  if (eh_pad_dims(m, &nxp, &nyp, &nzp) != EH_OK) return EH_EINVAL;
   const int nb = m->nb;
-  const int nxp = m->nx + 2 * nb, nyp = m->ny + 2 * nb, nzp = m->nz + 2 * nb;
-  float *xx = malloc((nxp + 1) * sizeof(float));
-  float *yy = malloc((nyp + 1) * sizeof(float));
-  float *zz = malloc((nzp + 1) * sizeof(float));
   padded_axis(m->nx, m->dx, m->ox, nb, m->lextend, xx);
   padded_axis(m->ny, m->dy, m->oy, nb, m->lextend, yy);
   padded_axis(m->nz, m->dz, m->oz, nb, m->lextend, zz);
-
-  /* padded model: interior copied (sigma = 1/rho for 11/22, rho for 33),
-   * edges replicated, nb air cells on top (regrid_init_free.c:82-141) */
   const size_t np = (size_t)nxp * nyp * nzp;
-  float *pad[3];
-  for (int a = 0; a < 3; a++) pad[a] = malloc(np * sizeof(float));
-#define PAD(a, i, j, k) pad[a][(i) + (size_t)nxp * ((j) + (size_t)nyp * (k))]
+#define PAD(a, i, j, k) pad[(size_t)(a) * np + (i) + (size_t)nxp * ((j) + (size_t)nyp * (k))]
   for (int k = 0; k < m->nz; k++)
     for (int j = 0; j < m->ny; j++)
       for (int i = 0; i < m->nx; i++) {
@@ -203,43 +204,60 @@ int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *g) {
         }
   }
 #undef PAD
-  int rc = EH_OK;
+  return EH_OK;
+}
+
+int eh_regrid_axes(const eh_model *m, const float *xx, const float *yy, const float *zz,
+                   float sx, float sy, float sz, eh_grid *g) {
+  int nxp, nyp, nzp;
+  if (!g || eh_pad_dims(m, &nxp, &nyp, &nzp) != EH_OK || m->n1 < 2 || m->n2 < 2 || m->n3 < 2)
+    return EH_EINVAL;
   centred_axis(m->n1, sx, xx[0], xx[nxp], m->d1min, g->x1);
   centred_axis(m->n2, sy, yy[0], yy[nyp], m->d2min, g->x2);
   /* z: input-model nodes down to 5 cells below the source, then stretched
    * to the bottom (regrid_init_free.c:190-205).  The reference sizes the
    * source search by nx (its line 194); it is reproduced, with a check that
    * the search stays on the padded z axis. */
-  const int k0 = find_index_checked(m->nx + 2 * nb, zz, nzp + 1, sz);
-  if (k0 < 0) {
-    rc = EH_ESEARCH;
-  } else {
-    const int np1 = k0 + 5, np2 = m->n3 - np1;
-    if (np1 > nzp || np2 < 1) {
-      rc = EH_EINVAL;
-    } else {
-      for (int i = 0; i <= np1; i++) g->x3[i] = zz[i];
-      float *x = malloc((np2 + 1) * sizeof(float));
-      eh_create_nugrid(np2, zz[nzp] - g->x3[np1], m->d3min, x);
-      for (int i = 0; i <= np2; i++) g->x3[np1 + i] = g->x3[np1] + x[i];
-      free(x);
-    }
-  }
+  const int k0 = find_index_checked(m->nx + 2 * m->nb, zz, nzp + 1, sz);
+  if (k0 < 0) return EH_ESEARCH;
+  const int np1 = k0 + 5, np2 = m->n3 - np1;
+  if (np1 > nzp || np2 < 1) return EH_EINVAL;
+  for (int i = 0; i <= np1; i++) g->x3[i] = zz[i];
+  float *x = malloc((np2 + 1) * sizeof(float));
+  eh_create_nugrid(np2, zz[nzp] - g->x3[np1], m->d3min, x);
+  for (int i = 0; i <= np2; i++) g->x3[np1 + i] = g->x3[np1] + x[i];
+  free(x);
+  eh_stagger(m->n1, g->x1, g->x1s, g->d1, g->d1s);
+  eh_stagger(m->n2, g->x2, g->x2s, g->d2, g->d2s);
+  eh_stagger(m->n3, g->x3, g->x3s, g->d3, g->d3s);
+  return EH_OK;
+}
+
+int eh_regrid(const eh_model *m, float sx, float sy, float sz, eh_grid *g) {
+  if (!m || !g || m->nx < 1 || m->ny < 1 || m->nz < 1 || m->nb < 0 || m->n1 < 2 || m->n2 < 2 ||
+      m->n3 < 2)
+    return EH_EINVAL;
+  int nxp, nyp, nzp;
+  eh_pad_dims(m, &nxp, &nyp, &nzp);
+  float *xx = malloc((nxp + 1) * sizeof(float));
+  float *yy = malloc((nyp + 1) * sizeof(float));
+  float *zz = malloc((nzp + 1) * sizeof(float));
+  const size_t np = (size_t)nxp * nyp * nzp;
+  float *pad = malloc(3 * np * sizeof(float));
+  int rc = eh_pad_model(m, xx, yy, zz, pad);
+  if (rc == EH_OK) rc = eh_regrid_axes(m, xx, yy, zz, sx, sy, sz, g);
   if (rc == EH_OK) {
-    eh_stagger(m->n1, g->x1, g->x1s, g->d1, g->d1s);
-    eh_stagger(m->n2, g->x2, g->x2s, g->d2, g->d2s);
-    eh_stagger(m->n3, g->x3, g->x3s, g->d3, g->d3s);
     float *outs[3] = {g->sigma11, g->sigma22, g->sigma33};
     for (int a = 0; a < 3 && rc == EH_OK; a++)
-      rc = eh_homogenize(pad[a], outs[a], nxp, nyp, nzp, xx, yy, zz, m->n1, m->n2, m->n3, g->x1,
-                         g->x2, g->x3);
+      rc = eh_homogenize(pad + (size_t)a * np, outs[a], nxp, nyp, nzp, xx, yy, zz, m->n1, m->n2,
+                         m->n3, g->x1, g->x2, g->x3);
     const size_t nc = (size_t)m->n1 * m->n2 * m->n3;
     for (size_t c = 0; c < nc; c++) {
       g->sigma33[c] = 1. / g->sigma33[c]; /* rho33 average -> sigma33 */
       g->invmur[c] = 1.;
     }
   }
-  for (int a = 0; a < 3; a++) free(pad[a]);
+  free(pad);
   free(xx);
   free(yy);
   free(zz);

@@ -639,7 +639,19 @@ void emmi_default_options(emmi_options* o) {
   o->line_factors = 2;
 }
 
+static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
+                       bool cells_on_device);
+
 int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_options* opts) {
+  return create_impl(out, P, opts, false);
+}
+
+int emmi_solver_create_dc(emmi_solver** out, const emmi_problem* P, const emmi_options* opts) {
+  return create_impl(out, P, opts, true);
+}
+
+static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
+                       bool cells_on_device) {
   if (!out || !P || !P->x1 || !P->x2 || !P->x3 || !P->cells || !P->omega) {
     set_err("emmi_solver_create: null argument");
     return EMMI_EINVAL;
@@ -817,7 +829,8 @@ int emmi_solver_create(emmi_solver** out, const emmi_problem* P, const emmi_opti
     const long nc0 = s->hier[0][0].ncell;
     float* raw = nullptr;
     TRY(s->alloc((void**)&raw, (size_t)s->nop * 4 * nc0 * sizeof(float)));
-    CKS(cudaMemcpyAsync(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    CKS(cudaMemcpyAsync(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float),
+                        cells_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->st));
     s->raw_cells = raw;
     // survey grids in float as emf_t holds them (regrid_init_free.c:21-34)
     {

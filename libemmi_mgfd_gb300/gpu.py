@@ -121,11 +121,18 @@ class Solver:
 
     def __init__(self, n: Sequence[int], x1, x2, x3, cells, omega, op=None,
                  options: Optional[Options] = None, rho_water=None):
+        """cells: a host array, or a device pointer (int, e.g. from
+        homogenize_batch) to float32 [nop, 4, n3, n2, n1]."""
         self.n = tuple(int(v) for v in n)
         self.x1 = np.ascontiguousarray(np.atleast_2d(x1), np.float32)
         self.x2 = np.ascontiguousarray(np.atleast_2d(x2), np.float32)
         self.x3 = np.ascontiguousarray(np.atleast_2d(x3), np.float32)
-        self.cells = np.ascontiguousarray(cells, np.float32).reshape(self.x1.shape[0], 4, -1)
+        dev_cells = isinstance(cells, int)
+        if dev_cells:
+            cells_ptr = cells
+        else:
+            self.cells = np.ascontiguousarray(cells, np.float32).reshape(self.x1.shape[0], 4, -1)
+            cells_ptr = _p(self.cells).value
         self.omega = np.ascontiguousarray(np.atleast_1d(omega), np.float32)
         self.nop = self.x1.shape[0]
         self.nrhs = self.omega.shape[0]
@@ -136,11 +143,12 @@ class Solver:
         self.rho_water = (np.zeros(self.nop, np.float32) if rho_water is None else
                           np.ascontiguousarray(np.broadcast_to(rho_water, (self.nop,)), np.float32))
         prob = _Problem(n1, n2, n3, self.nop, self.nrhs, _p(self.x1).value, _p(self.x2).value,
-                        _p(self.x3).value, _p(self.cells).value,
+                        _p(self.x3).value, cells_ptr,
                         None if self.op is None else _p(self.op).value, _p(self.omega).value,
                         _p(self.rho_water).value)
         h = C.c_void_p()
-        _check(lib().emmi_solver_create(C.byref(h), C.byref(prob), C.byref(self.options._c())),
+        create = lib().emmi_solver_create_dc if dev_cells else lib().emmi_solver_create
+        _check(create(C.byref(h), C.byref(prob), C.byref(self.options._c())),
                "emmi_solver_create")
         self._h = h
 
@@ -321,6 +329,24 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def homogenize_batch(padded, axes, n, cells_ptr: int, stream: int = 0):
+    """The device homogenization of a batch of shots: padded = (xx, yy, zz,
+    pad) of host.Model.padded(); axes = list of host.Model.axes() dicts;
+    writes float32 [nshots, 4, n3, n2, n1] at the device pointer cells_ptr
+    (emmi_homogenize_batch)."""
+    xx, yy, zz, pad = padded
+    nzp, nyp, nxp = pad.shape[1:]
+    n1, n2, n3 = (int(v) for v in n)
+    x1 = np.ascontiguousarray(np.stack([a["x1"] for a in axes]), np.float32)
+    x2 = np.ascontiguousarray(np.stack([a["x2"] for a in axes]), np.float32)
+    x3 = np.ascontiguousarray(np.stack([a["x3"] for a in axes]), np.float32)
+    pad = np.ascontiguousarray(pad, np.float32)
+    _check(lib().emmi_homogenize_batch(int(nxp), int(nyp), int(nzp), _p(xx), _p(yy), _p(zz),
+                                       _p(pad), len(axes), n1, n2, n3, _p(x1), _p(x2), _p(x3),
+                                       C.c_void_p(cells_ptr), C.c_void_p(stream)),
+           "emmi_homogenize_batch")
 
 
 def _level_args(n, x, cells):

@@ -133,6 +133,37 @@ class Model:
     def rho_water(self) -> float:
         return float(lib().eh_rho_water(C.byref(self._c())))
 
+    def padded(self):
+        """(xx, yy, zz, pad): the padded node axes and the padded model
+        [3, nzp, nyp, nxp] (sigma11, sigma22, rho33), once per model
+        (regrid_init_free.c:47-141)."""
+        m = self._c()
+        d = [C.c_int(), C.c_int(), C.c_int()]
+        if lib().eh_pad_dims(C.byref(m), *[C.byref(v) for v in d]) != 0:
+            raise RuntimeError("eh_pad_dims failed")
+        nxp, nyp, nzp = (v.value for v in d)
+        xx = np.zeros(nxp + 1, np.float32)
+        yy = np.zeros(nyp + 1, np.float32)
+        zz = np.zeros(nzp + 1, np.float32)
+        pad = np.zeros((3, nzp, nyp, nxp), np.float32)
+        if lib().eh_pad_model(C.byref(m), _ptr(xx), _ptr(yy), _ptr(zz), _ptr(pad)) != 0:
+            raise RuntimeError("eh_pad_model failed")
+        return xx, yy, zz, pad
+
+    def axes(self, xx, yy, zz, sx: float, sy: float, sz: float) -> dict:
+        """The mesh axes of a shot at (sx, sy, sz) and their staggered copies
+        (regrid_init_free.c:156-214), on the padded axes of padded()."""
+        out = {}
+        for nm in GRID_FIELDS[:12]:
+            n = {"1": self.n1, "2": self.n2, "3": self.n3}[nm[1]]
+            out[nm] = np.zeros(n + 1, np.float32)
+        g = _Grid(*([out[nm].ctypes.data for nm in GRID_FIELDS[:12]] + [None] * 4))
+        rc = lib().eh_regrid_axes(C.byref(self._c()), _ptr(xx), _ptr(yy), _ptr(zz), C.c_float(sx),
+                                  C.c_float(sy), C.c_float(sz), C.byref(g))
+        if rc != 0:
+            raise RuntimeError(f"eh_regrid_axes failed ({rc})")
+        return out
+
     def regrid(self, sx: float, sy: float, sz: float) -> dict:
         """Mesh and homogenized conductivities for a source at (sx, sy, sz)."""
         out = {}
