@@ -9,9 +9,11 @@ channels -- as one batch: inject the 25 sources, solve all 25 systems to
 |b - A x| <= 1e-8 |b| (FP64 residual), extract the receiver data.
 
   value  solves/s with the operators and right-hand sides resident in HBM
-  e2e    the same through the C ABI from host arrays: solver setup (H2D of
-         the 25 meshes and conductivity cubes), inject, solve, extract, D2H
-         of the receiver data
+  e2e    the same through the C ABI from the model on the host, as the
+         reference's modelling runs a shot (regrid, solve, extract): the
+         padded model and every shot's mesh axes on the host, H2D of the
+         padded model, the 25 shots' homogenization on the device, solver
+         setup, inject, solve, extract, D2H of the receiver data
   plain_fp64   the same batch with complex128 cycles (the reference's
          arithmetic), for the mixed-vs-plain ratio
   roofline     the level-0 line-relaxation sweep (dominant kernel), timed
@@ -120,7 +122,8 @@ def build_workload(n: int):
     rec = s.receivers.astype(np.float32).copy()
     rec[:, 3:] = np.deg2rad(rec[:, 3:])
     return dict(survey=s, X1=X1, X2=X2, X3=X3, cells=cells, omega=np.full(len(src), om, np.float32),
-                rho_water=np.float32(m.rho_water()), src=srcr, rec=rec, grids=grids)
+                rho_water=np.float32(m.rho_water()), src=srcr, rec=rec, grids=grids, model=m,
+                src_xyz=src[:, :3].copy())
 
 
 def make_solver(w, precision, tol, krylov=0):
@@ -382,12 +385,25 @@ def main():
 
     # e2e: from host arrays through the C ABI, solver setup included
     e2e_times, h2d, d2h = [], 0, 0
+    m = w["model"]
+    nsh = w["X1"].shape[0]
+    nc = int(np.prod(s.n))
+    dcells = torch.empty((nsh, 4, nc), dtype=torch.float32, device="cuda")
     for it in range(0 if a.no_e2e else 2):
         torch.cuda.synchronize()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record()
-        sv = make_solver(w, G.PREC_MIXED, a.tol, krylov=a.krylov)
+        # the front end: padded model and mesh axes on the host (1D work),
+        # the homogenization of every shot on the device
+        padded = m.padded()
+        axes = [m.axes(*padded[:3], float(p[0]), float(p[1]), float(p[2])) for p in w["src_xyz"]]
+        G.homogenize_batch(padded, axes, s.n, dcells.data_ptr())
+        X = [np.stack([ax[k] for ax in axes]) for k in ("x1", "x2", "x3")]
+        sv = G.Solver(s.n, *X, dcells.data_ptr(), w["omega"], op=np.arange(nsh, dtype=np.int32),
+                      options=G.Options(precision=G.PREC_MIXED, tol=a.tol, ncycle=100,
+                                        krylov=a.krylov),
+                      rho_water=w["rho_water"])
         if W is not None:
             sv.set_learned(W)  # the weights trained above, as a caller would reuse them
         _, _, (hb, db) = sv.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
@@ -396,7 +412,7 @@ def main():
         t1.synchronize()
         if it > 0:
             e2e_times.append(t0.elapsed_time(t1) / 1e3)
-        h2d = (w["X1"].nbytes + w["X2"].nbytes + w["X3"].nbytes + w["cells"].nbytes
+        h2d = (padded[3].nbytes + sum(v.nbytes for v in padded[:3]) + sum(x.nbytes for x in X)
                + w["omega"].nbytes + hb)
         d2h = db
     e2e = None
