@@ -1,7 +1,8 @@
 """Build the in-tree native libraries of the GB300 hot path.
 
   libemmi_gpu.so   CUDA kernels + batched solver + drop-in C ABI (nvcc, sm_103a)
-  libemmi_host.so  host front end in C (gcc): parameters, grids, homogenization
+  libemmi_host.so  host front end in C (gcc): parameters, grids, homogenization,
+                   l-BFGS / line search / regularization of the inversion
 
 Everything is compiled in-tree next to this file (no pip install), in
 parallel, with one -gencode for sm_103a.  nvcc cross-compiles without a GPU.
@@ -22,10 +23,10 @@ INCLUDE = os.path.join(ROOT, "include")
 
 GPU_SOURCES = ["emmi_kernels.cu", "emmi_solver.cu", "emmi_survey.cu", "emmi_dropin.cu",
                "emmi_krylov.cu", "emmi_learned.cu", "emmi_noalloc.cu", "emmi_frontend.cu"]
-HOST_SOURCES = ["emmi_host.c"]
+HOST_SOURCES = ["emmi_host.c", "emmi_fwi.c"]
 GPU_LIB = os.path.join(HERE, "libemmi_gpu.so")
 HOST_LIB = os.path.join(HERE, "libemmi_host.so")
-MAIN_SOURCES = ["emmi_main.c", "emmi_params.c", "emmi_host.c"]
+MAIN_SOURCES = ["emmi_main.c", "emmi_params.c", "emmi_host.c", "emmi_fwi.c"]
 MAIN_BIN = os.path.join(HERE, "emmi_main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE,

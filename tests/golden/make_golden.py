@@ -9,6 +9,7 @@ GPU machines; these fixtures carry its outputs there.
 
     python tests/golden/make_golden.py            (needs oracle/_ref built)
     python tests/golden/make_golden.py tiny_grad  (the mode=2 gradient case only)
+    python tests/golden/make_golden.py tiny_fwi   (the mode=1 inversion case only)
 """
 from __future__ import annotations
 
@@ -141,10 +142,85 @@ def mode2_case(tol="1e-10"):
     }
 
 
+def trace_lines(stdout):
+    """The lines of the inversion's stdout that record its path: the
+    iteration header, each evaluation's objective, the first-gradient
+    scaling and each failed Wolfe condition (src/do_fwi.c, src/opt.c,
+    src/fg_fwi.c)."""
+    keep = ("# iter=", "fcost=", "|x|_1=", "Wolfe condition")
+    return [l.strip() for l in stdout.splitlines() if l.strip().startswith(keep)]
+
+
+def mode1_case(tol="1e-10", niter=2, preco=1):
+    """The reference's main in mode=1 (the l-BFGS inversion, src/do_fwi.c)
+    for niter iterations from the start model of mode2_case, without noise:
+    iterate.txt, rmse_misfit.txt and the resistivities after every
+    iteration."""
+    true = W.tiny_layered()
+    start = start_model(true)
+    d = tempfile.mkdtemp(prefix="golden_m1_")
+    true.write(os.path.join(d, "true"))
+    start.write(d)
+    common = [f"tol={tol}", "ncycle=80"]
+    r0 = subprocess.run([REF_MAIN] + true.params(os.path.join(d, "true")) + common, cwd=d,
+                        capture_output=True, text=True)
+    if r0.returncode != 0:
+        raise RuntimeError(r0.stdout + r0.stderr)
+    obs_text = open(os.path.join(d, "emf_0001.txt")).read()
+    args = [a for a in start.params(d) if not a.startswith("mode=") and not a.startswith("verb=")]
+    args += ["mode=1", "verb=1", "addnoise=0", "npar=2", "idxpar=1,2", f"preco={preco}",
+             f"niter={niter}"] + common
+    r1 = subprocess.run([REF_MAIN] + args, cwd=d, capture_output=True, text=True)
+    if r1.returncode != 0:
+        raise RuntimeError(r1.stdout + r1.stderr)
+    n = start.nx * start.ny * start.nz
+    rec = {
+        "name": np.array("tiny_fwi"),
+        "params": np.array(" ".join(args[-7:])),
+        "rho_start": start.rho11,
+        "obs_text": np.array(obs_text),
+        "iterate": np.array(open(os.path.join(d, "iterate.txt")).read()),
+        "rmse_misfit": np.array(open(os.path.join(d, "rmse_misfit.txt")).read()),
+        "stdout": np.array(r1.stdout[-6000:]),
+        # every objective evaluation and line-search decision, in order
+        "trace": np.array("\n".join(trace_lines(r1.stdout))),
+    }
+    for it in range(niter):
+        for nm in ("Rv", "Rh"):
+            rec[f"{nm}_{it:02d}"] = np.fromfile(os.path.join(d, f"{nm}_iteration_{it:02d}"),
+                                                np.float32, n)
+    return rec
+
+
+def sensitivity(niter=2):
+    """How far the reference's own inversion moves when only the solver's
+    stopping tolerance changes (1e-10 against 1e-8): per preconditioner and
+    iteration, the largest log-resistivity difference between the two runs
+    beside the largest step from the start model."""
+    for preco in (1, 0, 2):
+        a = mode1_case(tol="1e-10", niter=niter, preco=preco)
+        b = mode1_case(tol="1e-8", niter=niter, preco=preco)
+        rho = np.asarray(a["rho_start"]).ravel()
+        for it in range(niter):
+            for nm in ("Rv", "Rh"):
+                x, y = a[f"{nm}_{it:02d}"], b[f"{nm}_{it:02d}"]
+                print(f"preco={preco} {nm} iteration {it}: max |dlog rho| "
+                      f"{np.abs(np.log(x) - np.log(y)).max():.3g}, step "
+                      f"{np.abs(np.log(x) - np.log(rho)).max():.3g}")
+
+
 def main():
     if not os.path.exists(REF_DUMP):
         sys.exit("oracle/_ref/ref_dump missing: run `make -C oracle ref` first")
     only = set(sys.argv[1:])
+    if only == {"sensitivity"}:
+        sensitivity()
+        return
+    if only == {"tiny_fwi"}:
+        rec = mode1_case()
+        np.savez_compressed(os.path.join(HERE, "tiny_fwi.npz"), **rec)
+        print("tiny_fwi", os.path.getsize(os.path.join(HERE, "tiny_fwi.npz")) // 1024, "KB")
+        return
     if only == {"tiny_grad"}:
         rec = mode2_case()
         np.savez_compressed(os.path.join(HERE, "tiny_grad.npz"), **rec)

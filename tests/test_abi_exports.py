@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
 PKG = os.path.join(ROOT, "libemmi_mgfd_gb300")
 LIBS = {"emmi_gpu.h": "libemmi_gpu.so", "emmi_dropin.h": "libemmi_gpu.so",
-        "emmi_host.h": "libemmi_host.so"}
+        "emmi_host.h": "libemmi_host.so", "emmi_fwi.h": "libemmi_host.so"}
 
 DECL = re.compile(r"^[A-Za-z_][\w \t\*]*?\b([A-Za-z_]\w*)\s*\(", re.M)
 
