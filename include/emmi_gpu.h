@@ -249,6 +249,74 @@ int emmi_build_gradient(int nx, int ny, int nz, const float o[3],
                         float dsmute, int nrec, const float *rec, float drmute,
                         float *grad, float *phess);
 
+/* ---- one objective evaluation of the inversion for a batch of shots ----
+ * fg_fwi (src/fg_fwi.c:139-290) with every shot and frequency in one
+ * solver: the homogenization of the current model for every shot, forward
+ * modelling, receiver data, data misfit and adjoint sources (the
+ * arithmetic of the host library's eh_misfit), adjoint modelling, and the
+ * gradient w.r.t. ln(rho) summed over shots and frequencies
+ * (build_gradient.c:13-113 with the MPI_Allreduce of fg_fwi.c:262-268), all
+ * on the device; per evaluation only the padded model and the input-grid
+ * resistivities go in and the gradient, misfits and data come out.  The
+ * model regularization, scaling and optimizer stay with the caller. */
+typedef struct {
+  int nx, ny, nz;       /* input model cells                                 */
+  float o[3], d[3];     /* its origin and cell sizes (emf->ox.., emf->dx..)  */
+  int n1, n2, n3;       /* multigrid mesh cells of every shot                */
+  int nshot, nfreq;     /* nshot * nfreq <= 65535 right-hand sides           */
+  const float *omega;   /* [nfreq] 2*pi*f (emf->omegas)                      */
+  const float *x1, *x2, *x3; /* [nshot][n+1] each shot's mesh axes
+                           (eh_regrid_axes of the host library)              */
+  float rho_water;      /* emf->rho_water of the start model                 */
+  int nsrc_ch;          /* source channels, codes 0..5 (Ex..Hz)              */
+  const int *src_ch;
+  int nrec_ch;          /* receiver channels                                 */
+  const int *rec_ch;
+  int nrec;             /* receivers per shot, the largest count             */
+  const int *nrec_shot; /* [nshot] each shot's receivers (<= nrec)           */
+  const float *src;     /* [nshot][5] x, y, z, azimuth, dip (radians)        */
+  const float *rec;     /* [nshot][nrec][5]                                  */
+  const float *dobs;    /* [nshot][nrec_ch][nfreq][nrec] complex, interleaved*/
+  const float *delta;   /* [nshot][nrec_ch][nfreq][nrec] uncertainties       */
+  int npar;             /* 1 or 2 parameters                                 */
+  const int *idxpar;    /* [npar] 1 = rho11/rho22, 2 = rho33                 */
+  int preco;            /* 1: also the pseudo-Hessian                        */
+  const float *bathy;   /* [ny][nx] sea-floor depth                          */
+  float dsmute, drmute; /* gradient mute half-widths around sources and
+                           receivers (fwi->dsmute, fwi->drmute)              */
+} emmi_fg_problem;
+
+/* the solver options gmg_init of the drop-in layer takes from the host's
+ * key=value parameters (cycleopt ncycle v1 v2 tol isemicoarsen gmg_precision
+ * sigma_floor, gmg.c:1712-1717, through getpar or emmi_gpu_set_param) */
+void emmi_dropin_options(emmi_options *o, int verb);
+
+typedef struct emmi_fg emmi_fg;
+/* copies the survey, data and masks to the device once per inversion */
+int emmi_fg_create(emmi_fg **out, const emmi_fg_problem *P,
+                   const emmi_options *opts);
+/* One evaluation at the model whose padded form is xx, yy, zz, pad
+ * (eh_pad_model) and whose input-grid resistivities are rho11, rho33
+ * [nz][ny][nx]: fcost [nshot] each shot's 0.5*|W(dobs - dcal)|^2, grad and
+ * phess (preco == 1; may be NULL) [npar][nz][ny][nx] summed over shots;
+ * dcal (complex, interleaved) and rmse (may be NULL) [nshot][nrec_ch]
+ * [nfreq][nrec]; stats (may be NULL) [2][nshot*nfreq], forward solves then
+ * adjoint.  Host arrays; synchronises. */
+int emmi_fg_eval(emmi_fg *f, int nxp, int nyp, int nzp, const float *xx,
+                 const float *yy, const float *zz, const float *pad,
+                 const float *rho11, const float *rho33, float *fcost,
+                 float *grad, float *phess, float *dcal, float *rmse,
+                 emmi_rhs_stats *stats);
+void emmi_fg_destroy(emmi_fg *f);
+/* The device misfit alone on host arrays (parity checks): per-shot arrays
+ * dobs, dcal, dres (complex, interleaved), delta, rmse [nshot][nch][nfreq]
+ * [nrec]; src [nshot][5], rec [nshot][nrec][5]; fcost [nshot]. */
+int emmi_misfit_batch(int nshot, int nch, int nfreq, int nrec,
+                      const int *nrec_shot, const float *omega, float rho_water,
+                      const float *src, const float *rec, const float *dobs,
+                      const float *delta, const float *dcal, float *dres,
+                      float *rmse, float *fcost);
+
 /* Interpolation of E (from x) or H (from h) to the input model's cell
  * centres (extract_electric_field / extract_magnetic_field,
  * inject_extract.c:477-785) for one RHS; host arrays, out [3][nz][ny][nx]

@@ -142,23 +142,28 @@ std::vector<float> receivers(const emmi_acq_t* acq) {
 
 extern "C" {
 
+// gmg.c:1712-1717: the multigrid knobs from the host's parameters
+void emmi_dropin_options(emmi_options* o, int verb) {
+  emmi_default_options(o);
+  o->cycleopt = (int)param("cycleopt", 2, true);
+  o->ncycle = (int)param("ncycle", 30, true);
+  o->v1 = (int)param("v1", 1, true);
+  o->v2 = (int)param("v2", 1, true);
+  o->tol = param("tol", 1e-6, false);
+  o->isemicoarsen = (int)param("isemicoarsen", 1, true);
+  o->precision = (int)param("gmg_precision", EMMI_PREC_MIXED, true);
+  o->sigma_floor = param("sigma_floor", 0.0, false);
+  o->verb = verb;
+}
+
 // gmg.c:1704-1733: knobs from the host's parameters, solver built here
 void gmg_init(emmi_emf_t* emf, int ifreq) {
   if (g.s) {
     emmi_solver_destroy(g.s);
     g.s = nullptr;
   }
-  emmi_default_options(&g.opt);
+  emmi_dropin_options(&g.opt, emf->verb);
   g.have_opt = true;
-  g.opt.cycleopt = (int)param("cycleopt", 2, true);
-  g.opt.ncycle = (int)param("ncycle", 30, true);
-  g.opt.v1 = (int)param("v1", 1, true);
-  g.opt.v2 = (int)param("v2", 1, true);
-  g.opt.tol = param("tol", 1e-6, false);
-  g.opt.isemicoarsen = (int)param("isemicoarsen", 1, true);
-  g.opt.precision = (int)param("gmg_precision", EMMI_PREC_MIXED, true);
-  g.opt.sigma_floor = param("sigma_floor", 0.0, false);
-  g.opt.verb = emf->verb;
   if (emf->verb) {
     printf("----------- gmg_init (GB300) ---------------\n");
     printf("cycleopt=%d ncycle=%d v1=%d v2=%d tol=%g isemicoarsen=%d precision=%s\n",

@@ -217,7 +217,6 @@ __global__ void __launch_bounds__(256) k_coef64(LevelView<double> L, double* __r
   const int op = blockIdx.y;
   const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (s >= L.S) return;
-  const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
   int P[3];
   slot_nodes(s, L, P);
   const double* cells = L.cells + (long)op * 4 * L.ncell;

@@ -218,6 +218,14 @@ typedef struct {
   int *chc;
   emmi_cf32 *Ef, *Ea, *dc;
   float *s11, *s22, *s33, *imu, *gsum, *hsum;
+  /* the batched evaluation on the device (batch=1): the padded model and
+   * its axes, each shot's misfit, data and rmse [nshot][nchrec][nfreq]
+   * [maxrec], solve statistics [2][nshot*nfreq] */
+  emmi_fg *fg;
+  int nxp, nyp, nzp, maxrec;
+  float *pxx, *pyy, *pzz, *pad, *fshot, *rall;
+  emmi_cf32 *dall;
+  emmi_rhs_stats *stats;
 } fg_ctx;
 
 /* point acq at the shot, regrid the current model around its source
@@ -241,6 +249,23 @@ static void set_shot(fg_ctx *c, shot_t *t) {
                emf->d1, emf->d2, emf->d3, emf->d1s, emf->d2s, emf->d3s,
                c->s11, c->s22, c->s33, c->imu};
   if (eh_regrid(c->M, t->src5[0], t->src5[1], t->src5[2], &G) != EH_OK) die("regrid failed", NULL);
+}
+
+/* rmse_%04d.txt of a shot: rmse [nchrec][nfreq][nrec] (write_rmse,
+ * src/read_write_data.c:80-102) */
+static void write_rmse(const emmi_emf_t *emf, const shot_t *t, const float *rmse) {
+  char fname[64];
+  snprintf(fname, sizeof(fname), "rmse_%04d.txt", t->shot);
+  FILE *fp = fopen(fname, "w");
+  if (!fp) die("cannot write ", fname);
+  fprintf(fp, "iTx iRx chrec frequency/Hz RMSE x y z\n");
+  for (int ic = 0; ic < emf->nchrec; ic++)
+    for (int f = 0; f < emf->nfreq; f++)
+      for (int ir = 0; ir < t->nrec; ir++)
+        fprintf(fp, "%d %d %s %g %e %g %g %g\n", t->shot, ir + 1, emf->chrec[ic], emf->freqs[f],
+                rmse[((size_t)ic * emf->nfreq + f) * t->nrec + ir], t->rx[ir], t->ry[ir],
+                t->rz[ir]);
+  fclose(fp);
 }
 
 /* forward modelling, misfit and adjoint sources, adjoint modelling and the
@@ -280,17 +305,7 @@ static float gradient_shot(fg_ctx *c, shot_t *t) {
                                 acq->src_x1[0], acq->src_x2[0], acq->rec_x1, acq->rec_x2,
                                 (const float *)t->dobs, (const float *)c->dc, t->delta,
                                 (float *)dres, rmse);
-  snprintf(fname, sizeof(fname), "rmse_%04d.txt", t->shot);
-  FILE *fp = fopen(fname, "w");
-  if (!fp) die("cannot write ", fname);
-  fprintf(fp, "iTx iRx chrec frequency/Hz RMSE x y z\n");
-  for (int ic = 0; ic < emf->nchrec; ic++)
-    for (int f = 0; f < nf; f++)
-      for (int ir = 0; ir < nrec; ir++)
-        fprintf(fp, "%d %d %s %g %e %g %g %g\n", t->shot, ir + 1, emf->chrec[ic], emf->freqs[f],
-                rmse[((size_t)ic * nf + f) * nrec + ir], acq->rec_x1[ir], acq->rec_x2[ir],
-                acq->rec_x3[ir]);
-  fclose(fp);
+  write_rmse(emf, t, rmse);
   const int ndat = emf->nchrec * nf * nrec;
   if (emf->verb) printf("isrc=%d, fcost=%g, rmse=%g\n", t->shot, fcost, sqrt(2. * fcost / ndat));
   emf->E1 = E1a;
@@ -316,6 +331,171 @@ static float gradient_shot(fg_ctx *c, shot_t *t) {
   free(dres);
   free(rmse);
   return fcost;
+}
+
+/* the batched evaluation (batch=1): every shot's mesh axes (the padded
+ * model's node axes do not depend on the resistivities), the survey, the
+ * observed data and the uncertainties go to the device once */
+static void fg_batch_init(fg_ctx *c) {
+  emmi_emf_t *emf = c->emf;
+  emmi_fwi_t *fwi = c->fwi;
+  const int ns = c->nshots, nf = emf->nfreq, nch = emf->nchrec;
+  const int n1 = emf->n1, n2 = emf->n2, n3 = emf->n3;
+  if (eh_pad_dims(c->M, &c->nxp, &c->nyp, &c->nzp) != EH_OK) die("eh_pad_dims failed", NULL);
+  c->pxx = malloc((c->nxp + 1) * sizeof(float));
+  c->pyy = malloc((c->nyp + 1) * sizeof(float));
+  c->pzz = malloc((c->nzp + 1) * sizeof(float));
+  c->pad = malloc((size_t)3 * c->nxp * c->nyp * c->nzp * sizeof(float));
+  if (eh_pad_model(c->M, c->pxx, c->pyy, c->pzz, c->pad) != EH_OK) die("eh_pad_model failed", NULL);
+  int maxrec = 1;
+  for (int is = 0; is < ns; is++)
+    if (c->sh[is].nrec > maxrec) maxrec = c->sh[is].nrec;
+  c->maxrec = maxrec;
+  float *ax[3] = {malloc((size_t)ns * (n1 + 1) * sizeof(float)),
+                  malloc((size_t)ns * (n2 + 1) * sizeof(float)),
+                  malloc((size_t)ns * (n3 + 1) * sizeof(float))};
+  float *tmp = malloc((size_t)9 * (n1 + n2 + n3 + 3) * sizeof(float));
+  float *src = calloc((size_t)ns * 5, sizeof(float));
+  float *rec = calloc((size_t)ns * maxrec * 5, sizeof(float));
+  int *nrs = malloc(ns * sizeof(int));
+  const size_t nper = (size_t)ns * nch * nf * maxrec;
+  emmi_cf32 *dobs = calloc(nper, sizeof(emmi_cf32));
+  float *delta = calloc(nper, sizeof(float));
+  for (int is = 0; is < ns; is++) {
+    const shot_t *t = &c->sh[is];
+    float *q = tmp;
+    eh_grid g;
+    memset(&g, 0, sizeof(g));
+    g.x1 = ax[0] + (size_t)is * (n1 + 1);
+    g.x2 = ax[1] + (size_t)is * (n2 + 1);
+    g.x3 = ax[2] + (size_t)is * (n3 + 1);
+    float **rest[9] = {&g.x1s, &g.x2s, &g.x3s, &g.d1, &g.d2, &g.d3, &g.d1s, &g.d2s, &g.d3s};
+    const int len[3] = {n1 + 1, n2 + 1, n3 + 1};
+    for (int k = 0; k < 9; k++) {
+      *rest[k] = q;
+      q += len[k % 3];
+    }
+    if (eh_regrid_axes(c->M, c->pxx, c->pyy, c->pzz, t->src5[0], t->src5[1], t->src5[2], &g) !=
+        EH_OK)
+      die("eh_regrid_axes failed", NULL);
+    memcpy(src + (size_t)is * 5, t->src5, 5 * sizeof(float));
+    nrs[is] = t->nrec;
+    for (int ir = 0; ir < t->nrec; ir++) {
+      float *p = rec + ((size_t)is * maxrec + ir) * 5;
+      p[0] = t->rx[ir];
+      p[1] = t->ry[ir];
+      p[2] = t->rz[ir];
+      p[3] = t->raz[ir];
+      p[4] = t->rdip[ir];
+    }
+    for (int ic = 0; ic < nch; ic++)
+      for (int f = 0; f < nf; f++)
+        for (int ir = 0; ir < t->nrec; ir++) {
+          const size_t from = ((size_t)ic * nf + f) * t->nrec + ir;
+          const size_t to = (((size_t)is * nch + ic) * nf + f) * maxrec + ir;
+          dobs[to] = t->dobs[from];
+          delta[to] = t->delta[from];
+        }
+  }
+  int *src_ch = malloc(emf->nchsrc * sizeof(int));
+  for (int k = 0; k < emf->nchsrc; k++) src_ch[k] = chan_code(emf->chsrc[k]);
+  emmi_fg_problem P;
+  memset(&P, 0, sizeof(P));
+  P.nx = emf->nx;
+  P.ny = emf->ny;
+  P.nz = emf->nz;
+  P.o[0] = emf->ox;
+  P.o[1] = emf->oy;
+  P.o[2] = emf->oz;
+  P.d[0] = emf->dx;
+  P.d[1] = emf->dy;
+  P.d[2] = emf->dz;
+  P.n1 = n1;
+  P.n2 = n2;
+  P.n3 = n3;
+  P.nshot = ns;
+  P.nfreq = nf;
+  P.omega = emf->omegas;
+  P.x1 = ax[0];
+  P.x2 = ax[1];
+  P.x3 = ax[2];
+  P.rho_water = emf->rho_water;
+  P.nsrc_ch = emf->nchsrc;
+  P.src_ch = src_ch;
+  P.nrec_ch = nch;
+  P.rec_ch = c->chc;
+  P.nrec = maxrec;
+  P.nrec_shot = nrs;
+  P.src = src;
+  P.rec = rec;
+  P.dobs = (const float *)dobs;
+  P.delta = delta;
+  P.npar = fwi->npar;
+  P.idxpar = fwi->idxpar;
+  P.preco = fwi->preco;
+  P.bathy = &emf->bathy[0][0];
+  P.dsmute = emf->dsmute;
+  P.drmute = emf->drmute;
+  emmi_options opt;
+  emmi_dropin_options(&opt, 0);
+  if (emmi_fg_create(&c->fg, &P, &opt) != EMMI_OK) die("emmi_fg_create failed: ", emmi_last_error());
+  c->fshot = malloc(ns * sizeof(float));
+  c->rall = malloc(nper * sizeof(float));
+  c->dall = malloc(nper * sizeof(emmi_cf32));
+  c->stats = malloc((size_t)2 * ns * nf * sizeof(emmi_rhs_stats));
+  for (int k = 0; k < 3; k++) free(ax[k]);
+  free(tmp);
+  free(src);
+  free(rec);
+  free(nrs);
+  free(dobs);
+  free(delta);
+  free(src_ch);
+}
+
+/* the data part of fg_fwi for every shot in one device evaluation: the
+ * shot-summed gradient into c->gsum (pseudo-Hessian into c->hsum), each
+ * shot's syn_ and rmse_ files and misfit line; returns the summed misfit */
+static float fg_batch(fg_ctx *c) {
+  emmi_emf_t *emf = c->emf;
+  const int nf = emf->nfreq, nch = emf->nchrec;
+  if (eh_pad_model(c->M, c->pxx, c->pyy, c->pzz, c->pad) != EH_OK) die("eh_pad_model failed", NULL);
+  if (emmi_fg_eval(c->fg, c->nxp, c->nyp, c->nzp, c->pxx, c->pyy, c->pzz, c->pad,
+                   &emf->rho11[0][0][0], &emf->rho33[0][0][0], c->fshot, c->gsum,
+                   c->fwi->preco == 1 ? c->hsum : NULL, (float *)c->dall, c->rall,
+                   c->stats) != EMMI_OK)
+    die("emmi_fg_eval failed: ", emmi_last_error());
+  float fcost_dat = 0;
+  float *rm = malloc((size_t)nch * nf * c->maxrec * sizeof(float));
+  for (int is = 0; is < c->nshots; is++) {
+    const shot_t *t = &c->sh[is];
+    if (emf->verb)
+      for (int a = 0; a < 2; a++)
+        for (int f = 0; f < nf; f++) {
+          const emmi_rhs_stats *q = &c->stats[((size_t)a * c->nshots + is) * nf + f];
+          printf("shot %d freq %g%s: %d cycles, relative residual %.3e, status %d\n", t->shot,
+                 emf->freqs[f], a ? " (adjoint)" : "", q->cycles,
+                 q->rnorm0 > 0 ? q->rnorm / q->rnorm0 : 0., q->status);
+        }
+    for (int ic = 0; ic < nch; ic++)
+      for (int f = 0; f < nf; f++)
+        for (int ir = 0; ir < t->nrec; ir++) {
+          const size_t from = (((size_t)is * nch + ic) * nf + f) * c->maxrec + ir;
+          const size_t to = ((size_t)ic * nf + f) * t->nrec + ir;
+          c->dc[to] = c->dall[from];
+          rm[to] = c->rall[from];
+        }
+    char fname[64];
+    snprintf(fname, sizeof(fname), "syn_%04d.txt", t->shot);
+    write_data(fname, t->shot, emf, t->nrec, c->dc);
+    write_rmse(emf, t, rm);
+    const int ndat = nch * nf * t->nrec;
+    if (emf->verb)
+      printf("isrc=%d, fcost=%g, rmse=%g\n", t->shot, c->fshot[is], sqrt(2. * c->fshot[is] / ndat));
+    fcost_dat += c->fshot[is];
+  }
+  free(rm);
+  return fcost_dat;
 }
 
 static void write_floats(const char *name, const float *a, size_t n) {
@@ -395,12 +575,16 @@ static float fg_eval(void *ctx, float *xx, float *g) {
   memset(c->gsum, 0, fwi->n * sizeof(float));
   memset(c->hsum, 0, fwi->n * sizeof(float));
   float fcost_dat = 0;
-  for (int is = 0; is < c->nshots; is++) {
-    set_shot(c, &c->sh[is]);
-    fcost_dat += gradient_shot(c, &c->sh[is]);
-    for (long i = 0; i < fwi->n; i++) {
-      c->gsum[i] += (&fwi->grad[0][0][0][0])[i];
-      if (fwi->preco == 1) c->hsum[i] += (&fwi->phess[0][0][0][0])[i];
+  if (c->fg) {
+    fcost_dat = fg_batch(c);
+  } else {
+    for (int is = 0; is < c->nshots; is++) {
+      set_shot(c, &c->sh[is]);
+      fcost_dat += gradient_shot(c, &c->sh[is]);
+      for (long i = 0; i < fwi->n; i++) {
+        c->gsum[i] += (&fwi->grad[0][0][0][0])[i];
+        if (fwi->preco == 1) c->hsum[i] += (&fwi->phess[0][0][0][0])[i];
+      }
     }
   }
   /* the shot sums (the reference's MPI_Allreduce, src/fg_fwi.c:262-268) */
@@ -850,6 +1034,11 @@ int main(int argc, char **argv) {
     write_data(fname, t->shot, &emf, t->nrec, t->dobs);
     c.ndata += emf.nchrec * emf.nfreq * t->nrec;
   }
+  /* batch=1 (default): all shots and frequencies of an evaluation in one
+   * device solver; batch=0: shot by shot through the drop-in entry points */
+  int batch = 1;
+  getparint("batch", &batch);
+  if (batch) fg_batch_init(&c);
   if (emf.mode == 2) {
     /* one misfit and gradient at the input model (x = log rho, do_fwi.c:113-124) */
     float *xx = malloc((size_t)fwi.n * sizeof(float)), *g = malloc((size_t)fwi.n * sizeof(float));
@@ -863,5 +1052,6 @@ int main(int argc, char **argv) {
   } else {
     do_fwi(&c);
   }
+  if (c.fg) emmi_fg_destroy(c.fg);
   return 0;
 }

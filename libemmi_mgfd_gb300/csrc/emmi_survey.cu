@@ -316,11 +316,13 @@ __global__ void k_extract_receivers(SGrid G0, int gstride, const int* __restrict
 }
 
 // interpolation to input-model cell centres for one RHS
-// (inject_extract.c:477-635 for E, 638-785 for H)
+// (inject_extract.c:477-635 for E, 638-785 for H); component c of the cell
+// id goes to out[c * cstride + id]
 __global__ void k_extract_volume(SGrid G, int which, int nx, int ny, int nz, float ox, float oy,
                                  float oz, float dx, float dy, float dz,
                                  const float* __restrict__ rho33, const float* __restrict__ sig33,
-                                 const double2* __restrict__ fld, float2* __restrict__ out) {
+                                 const double2* __restrict__ fld, float2* __restrict__ out,
+                                 long cstride) {
   const long nxyz = (long)nx * ny * nz;
   const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (id >= nxyz) return;
@@ -370,7 +372,7 @@ __global__ void k_extract_volume(SGrid G, int which, int nx, int ny, int nz, flo
     } else {
       s = gather8(G.n, c, t, fld, nullptr);
     }
-    out[c * nxyz + id] = make_float2((float)s.re, (float)s.im);
+    out[c * cstride + id] = make_float2((float)s.re, (float)s.im);
   }
 }
 
@@ -433,7 +435,106 @@ __global__ void k_gradient(int nxyz, int nshot, int nfreq, int npar, const int* 
   }
 }
 
+// data misfit and adjoint sources (fg_fwi.c:208-226, in the arithmetic of
+// the host library's eh_misfit), one block per shot.  Per datum (channel c,
+// frequency f, receiver ir < nrec_shot) farther than skin[f] from the
+// source: r = (dobs - dcal) / delta, rmse = |r|, adjoint source
+// conj(r / delta), and term = |r|^2 in double: the reference's r * conj(r)
+// multiplies by the double-complex conj, so each term is a double and the
+// float cost advances by a double addition rounded to float.  The shot's
+// cost, 0.5 * the sum in the reference's loop order, by one thread.  Per-shot arrays
+// (dobs, delta, rmse, dsyn, term) are [nshot][nch][nfreq][nrec]; per-RHS
+// arrays (dcal, dres) [nshot * nfreq][nch][nrec], src [nshot * nfreq][5],
+// rec [nshot * nfreq][nrec][5]
+__global__ void k_misfit(int nch, int nfreq, int nrec, const int* __restrict__ nrec_shot,
+                         const float* __restrict__ skin, const float* __restrict__ src,
+                         const float* __restrict__ rec, const float2* __restrict__ dobs,
+                         const float* __restrict__ delta, const float2* __restrict__ dcal,
+                         float2* __restrict__ dres, float* __restrict__ rmse,
+                         float2* __restrict__ dsyn, double* __restrict__ term,
+                         float* __restrict__ fcost) {
+  const int sh = blockIdx.x;
+  const int nr = nrec_shot[sh];
+  const long nd = (long)nch * nfreq * nrec;
+  for (long i = threadIdx.x; i < nd; i += blockDim.x) {
+    const int ir = (int)(i % nrec), f = (int)((i / nrec) % nfreq), c = (int)(i / ((long)nrec * nfreq));
+    const long q = (long)sh * nd + i;
+    const long rr = (long)sh * nfreq + f;
+    const long k = (rr * nch + c) * nrec + ir;
+    const float2 dc = dcal[k];
+    float2 out = make_float2(0.f, 0.f);
+    float rm = 0.f;
+    double t = 0.;
+    if (ir < nr) {
+      const float* p = rec + (rr * nrec + ir) * 5;
+      const float* s0 = src + rr * 5;
+      const float ox = __fsub_rn(p[0], s0[0]), oy = __fsub_rn(p[1], s0[1]);
+      const float r2 = __fadd_rn(__fmul_rn(ox, ox), __fmul_rn(oy, oy));
+      if (sqrt((double)r2) > (double)skin[f]) {
+        const float dl = delta[q];
+        const float2 ob = dobs[q];
+        float re = __fdiv_rn(__fsub_rn(ob.x, dc.x), dl);
+        float im = __fdiv_rn(__fsub_rn(ob.y, dc.y), dl);
+        rm = (float)sqrt(__dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
+        t = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+        re = __fdiv_rn(re, dl);
+        im = __fdiv_rn(im, dl);
+        out = make_float2(re, -im);
+      }
+    }
+    dres[k] = out;
+    rmse[q] = rm;
+    term[q] = t;
+    dsyn[q] = dc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float acc = 0.f;
+    for (long i = 0; i < nd; i++) acc = (float)__dadd_rn((double)acc, term[(long)sh * nd + i]);
+    fcost[sh] = __fmul_rn(acc, 0.5f);
+  }
+}
+
 inline unsigned nblk(long n, int bs = 256) { return (unsigned)std::max<long>(1, (n + bs - 1) / bs); }
+
+// gradient masks (build_gradient.c:50-111, with the reference's float-to-int
+// truncation): bm[cell] = 1 at and above the sea floor plus one cell;
+// mm[shot][cell] = 1 in the boxes of half-width dsmute around the shot's
+// source and drmute around each of its receivers.  src: [nshot] points,
+// rec: [nshot][nrec] points, stride floats apart (x, y, z first);
+// nrec_shot (optional): receivers of each shot
+void gradient_masks(int nx, int ny, int nz, const float o[3], const float d[3], const float* bathy,
+                    int nshot, const float* src, float dsmute, int nrec, const int* nrec_shot,
+                    const float* rec, float drmute, int stride, std::vector<unsigned char>& bm,
+                    std::vector<unsigned char>& mm) {
+  const long nxyz = (long)nx * ny * nz;
+  bm.assign(nxyz, 0);
+  mm.assign((size_t)nshot * nxyz, 0);
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++)
+        if (o[2] + (k + 0.5) * d[2] <= bathy[i + (long)nx * j] + d[2])
+          bm[i + (long)nx * (j + (long)ny * k)] = 1;
+  const int nn[3] = {nx, ny, nz};
+  auto paint = [&](int sh, const float* p, float rad) {
+    int lo[3], hi[3];
+    for (int e = 0; e < 3; e++) {
+      lo[e] = (int)((p[e] - rad - o[e]) / d[e]);
+      hi[e] = (int)((p[e] + rad - o[e]) / d[e]);
+      lo[e] = std::min(std::max(lo[e], 0), nn[e] - 1);
+      hi[e] = std::min(std::max(hi[e], 0), nn[e] - 1);
+    }
+    for (int k = lo[2]; k <= hi[2]; k++)
+      for (int j = lo[1]; j <= hi[1]; j++)
+        for (int i = lo[0]; i <= hi[0]; i++)
+          mm[(size_t)sh * nxyz + i + (long)nx * (j + (long)ny * k)] = 1;
+  };
+  for (int sh = 0; sh < nshot; sh++) {
+    paint(sh, src + (long)stride * sh, dsmute);
+    const int nr = nrec_shot ? nrec_shot[sh] : nrec;
+    for (int ir = 0; ir < nr; ir++) paint(sh, rec + (long)stride * ((long)sh * nrec + ir), drmute);
+  }
+}
 
 ChanList make_chans(int n, const int* ch) {
   ChanList c;
@@ -576,7 +677,7 @@ int emmi_extract_volume(emmi_solver* s, int rhs, int which, int nx, int ny, int 
   k_extract_volume<<<nblk(nxyz), 256, 0, s->st>>>(G, which, nx, ny, nz, o[0], o[1], o[2], d[0],
                                                    d[1], d[2], drho,
                                                    s->raw_cells + ((long)op * 4 + 2) * nc, df,
-                                                   dout);
+                                                   dout, nxyz);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, dout, 3 * nxyz * sizeof(float2), cudaMemcpyDeviceToHost, s->st));
   cudaFreeAsync(df, s->st);
@@ -599,32 +700,9 @@ int emmi_build_gradient(int nx, int ny, int nz, const float o[3], const float d[
     return EMMI_EINVAL;
   }
   const long nxyz = (long)nx * ny * nz;
-  // masks on the host: bathymetry (shared) and per-shot boxes
-  // (build_gradient.c:50-111, with the reference's float-to-int truncation)
-  std::vector<unsigned char> bm(nxyz, 0), mm((size_t)nshot * nxyz, 0);
-  for (int k = 0; k < nz; k++)
-    for (int j = 0; j < ny; j++)
-      for (int i = 0; i < nx; i++)
-        if (o[2] + (k + 0.5) * d[2] <= bathy[i + (long)nx * j] + d[2])
-          bm[i + (long)nx * (j + (long)ny * k)] = 1;
-  const int nn[3] = {nx, ny, nz};
-  auto paint = [&](int sh, const float* p, float rad) {
-    int lo[3], hi[3];
-    for (int e = 0; e < 3; e++) {
-      lo[e] = (int)((p[e] - rad - o[e]) / d[e]);
-      hi[e] = (int)((p[e] + rad - o[e]) / d[e]);
-      lo[e] = std::min(std::max(lo[e], 0), nn[e] - 1);
-      hi[e] = std::min(std::max(hi[e], 0), nn[e] - 1);
-    }
-    for (int k = lo[2]; k <= hi[2]; k++)
-      for (int j = lo[1]; j <= hi[1]; j++)
-        for (int i = lo[0]; i <= hi[0]; i++)
-          mm[(size_t)sh * nxyz + i + (long)nx * (j + (long)ny * k)] = 1;
-  };
-  for (int sh = 0; sh < nshot; sh++) {
-    paint(sh, src + 3 * sh, dsmute);
-    for (int ir = 0; ir < nrec; ir++) paint(sh, rec + 3 * ((long)sh * nrec + ir), drmute);
-  }
+  std::vector<unsigned char> bm, mm;
+  gradient_masks(nx, ny, nz, o, d, bathy, nshot, src, dsmute, nrec, nullptr, rec, drmute, 3, bm,
+                 mm);
   const size_t ef = (size_t)nshot * nfreq * nxyz * sizeof(float2);
   cudaStream_t st;
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -663,6 +741,342 @@ int emmi_build_gradient(int nx, int ny, int nz, const float o[3], const float d[
   if (didx) cudaFreeAsync(didx, st);
   cudaStreamSynchronize(st);
   cudaStreamDestroy(st);
+  return rc;
+}
+
+}  // extern "C"
+
+// ---- the inversion's misfit-and-gradient evaluation for a batch of shots --
+
+// the skin-depth offset below which data are left out of the misfit,
+// 5.5 skin depths in water (fg_fwi.c:212, the arithmetic of eh_misfit)
+static float misfit_skin(float omega, float rho_water) {
+  const double mu0 = 4. * 3.14159265358979323846264 * 1e-7;
+  return 5.5 * sqrt(2. * rho_water / (omega * mu0));
+}
+
+// per-RHS copies of each shot's source and receivers: RHS r = shot * nfreq
+// + f; receivers past a shot's count repeat its first receiver (their data
+// and adjoint sources are zero) so that every interpolation stays inside
+static void per_rhs_points(int nshot, int nfreq, int nrec, const int* nrec_shot, const float* src,
+                           const float* rec, std::vector<float>& rsrc, std::vector<float>& rrec) {
+  const int nrhs = nshot * nfreq;
+  rsrc.assign((size_t)nrhs * 5, 0.f);
+  rrec.assign((size_t)nrhs * std::max(nrec, 1) * 5, 0.f);
+  for (int r = 0; r < nrhs; r++) {
+    const int sh = r / nfreq;
+    std::memcpy(&rsrc[(size_t)r * 5], src + (size_t)sh * 5, 5 * sizeof(float));
+    const int nr = nrec_shot ? nrec_shot[sh] : nrec;
+    for (int ir = 0; ir < nrec; ir++) {
+      const float* p = ir < nr ? rec + ((size_t)sh * nrec + ir) * 5
+                               : (nr > 0 ? rec + (size_t)sh * nrec * 5 : src + (size_t)sh * 5);
+      std::memcpy(&rrec[((size_t)r * nrec + ir) * 5], p, 5 * sizeof(float));
+    }
+  }
+}
+
+struct emmi_fg {
+  int nx, ny, nz, n1, n2, n3, nshot, nfreq, nrhs, nrec, nch, nsrc_ch, npar, preco;
+  float o[3], d[3], rho_water;
+  long nxyz, nc;
+  std::vector<float> x1, x2, x3, omega_rhs, rho_water_op;
+  std::vector<int> op, src_ch, rec_ch, idxpar;
+  emmi_options opt;
+  cudaStream_t st = nullptr;
+  float *d_src = nullptr, *d_rec = nullptr, *d_delta = nullptr, *d_skin = nullptr;
+  float *d_rmse = nullptr, *d_fcost = nullptr, *d_rho11 = nullptr;
+  double* d_term = nullptr;
+  float *d_rho33 = nullptr, *d_grad = nullptr, *d_phess = nullptr, *d_cells = nullptr;
+  float2 *d_dobs = nullptr, *d_dcal = nullptr, *d_dres = nullptr, *d_dsyn = nullptr;
+  float2 *d_Ef = nullptr, *d_Ea = nullptr;
+  unsigned char *d_bm = nullptr, *d_mm = nullptr;
+  int *d_nrec = nullptr, *d_idx = nullptr;
+  std::vector<void*> owned;
+  template <typename T>
+  bool alloc(T** p, size_t n) {
+    if (cudaMallocAsync((void**)p, n * sizeof(T) + 16, st) != cudaSuccess) return false;
+    owned.push_back(*p);
+    return true;
+  }
+};
+
+extern "C" {
+
+void emmi_fg_destroy(emmi_fg* f) {
+  if (!f) return;
+  for (void* p : f->owned) cudaFreeAsync(p, f->st);
+  if (f->st) {
+    cudaStreamSynchronize(f->st);
+    cudaStreamDestroy(f->st);
+  }
+  delete f;
+}
+
+int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* opts) {
+  if (!out || !P || !opts) {
+    set_err("emmi_fg_create: bad argument");
+    return EMMI_EINVAL;
+  }
+  *out = nullptr;
+  bool ok = P->nx > 0 && P->ny > 0 && P->nz > 0 && P->n1 > 0 && P->n2 > 0 && P->n3 > 0 &&
+            P->nshot > 0 && P->nfreq > 0 && (long)P->nshot * P->nfreq <= 65535 && P->omega &&
+            P->x1 && P->x2 && P->x3 && P->nsrc_ch >= 1 && P->nsrc_ch <= 6 && P->src_ch &&
+            P->nrec_ch >= 1 && P->nrec_ch <= 6 && P->rec_ch && P->nrec >= 1 && P->nrec_shot &&
+            P->src && P->rec && P->dobs && P->delta && P->npar >= 1 && P->npar <= 2 &&
+            P->idxpar && P->bathy && P->rho_water > 0;
+  for (int k = 0; ok && k < P->npar; k++) ok = P->idxpar[k] == 1 || P->idxpar[k] == 2;
+  for (int k = 0; ok && k < P->nsrc_ch; k++) ok = P->src_ch[k] >= 0 && P->src_ch[k] <= 5;
+  for (int k = 0; ok && k < P->nrec_ch; k++) ok = P->rec_ch[k] >= 0 && P->rec_ch[k] <= 5;
+  for (int k = 0; ok && k < P->nshot; k++) ok = P->nrec_shot[k] >= 0 && P->nrec_shot[k] <= P->nrec;
+  if (!ok) {
+    set_err("emmi_fg_create: bad problem description");
+    return EMMI_EINVAL;
+  }
+  emmi_fg* f = new emmi_fg();
+  f->nx = P->nx;
+  f->ny = P->ny;
+  f->nz = P->nz;
+  f->n1 = P->n1;
+  f->n2 = P->n2;
+  f->n3 = P->n3;
+  f->nshot = P->nshot;
+  f->nfreq = P->nfreq;
+  f->nrhs = P->nshot * P->nfreq;
+  f->nrec = P->nrec;
+  f->nch = P->nrec_ch;
+  f->nsrc_ch = P->nsrc_ch;
+  f->npar = P->npar;
+  f->preco = P->preco;
+  f->rho_water = P->rho_water;
+  for (int e = 0; e < 3; e++) {
+    f->o[e] = P->o[e];
+    f->d[e] = P->d[e];
+  }
+  f->nxyz = (long)P->nx * P->ny * P->nz;
+  f->nc = (long)P->n1 * P->n2 * P->n3;
+  f->x1.assign(P->x1, P->x1 + (size_t)P->nshot * (P->n1 + 1));
+  f->x2.assign(P->x2, P->x2 + (size_t)P->nshot * (P->n2 + 1));
+  f->x3.assign(P->x3, P->x3 + (size_t)P->nshot * (P->n3 + 1));
+  f->rho_water_op.assign(P->nshot, P->rho_water);
+  f->src_ch.assign(P->src_ch, P->src_ch + P->nsrc_ch);
+  f->rec_ch.assign(P->rec_ch, P->rec_ch + P->nrec_ch);
+  f->idxpar.assign(P->idxpar, P->idxpar + P->npar);
+  for (int r = 0; r < f->nrhs; r++) {
+    f->op.push_back(r / P->nfreq);
+    f->omega_rhs.push_back(P->omega[r % P->nfreq]);
+  }
+  f->opt = *opts;
+  std::vector<float> skin(P->nfreq), rsrc, rrec;
+  for (int k = 0; k < P->nfreq; k++) skin[k] = misfit_skin(P->omega[k], P->rho_water);
+  per_rhs_points(P->nshot, P->nfreq, P->nrec, P->nrec_shot, P->src, P->rec, rsrc, rrec);
+  std::vector<unsigned char> bm, mm;
+  gradient_masks(P->nx, P->ny, P->nz, P->o, P->d, P->bathy, P->nshot, P->src, P->dsmute,
+                 P->nrec, P->nrec_shot, P->rec, P->drmute, 5, bm, mm);
+  const size_t nper = (size_t)P->nshot * f->nch * P->nfreq * P->nrec;
+  const size_t nrd = (size_t)f->nrhs * f->nch * P->nrec;
+  const size_t ne = (size_t)3 * f->nrhs * f->nxyz;
+  if (cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking) != cudaSuccess ||
+      !f->alloc(&f->d_src, rsrc.size()) || !f->alloc(&f->d_rec, rrec.size()) ||
+      !f->alloc(&f->d_delta, nper) || !f->alloc(&f->d_skin, P->nfreq) ||
+      !f->alloc(&f->d_rmse, nper) || !f->alloc(&f->d_term, nper) ||
+      !f->alloc(&f->d_fcost, P->nshot) || !f->alloc(&f->d_rho11, f->nxyz) ||
+      !f->alloc(&f->d_rho33, f->nxyz) || !f->alloc(&f->d_grad, (size_t)P->npar * f->nxyz) ||
+      !f->alloc(&f->d_phess, (size_t)P->npar * f->nxyz) ||
+      !f->alloc(&f->d_cells, (size_t)P->nshot * 4 * f->nc) || !f->alloc(&f->d_dobs, nper) ||
+      !f->alloc(&f->d_dcal, nrd) || !f->alloc(&f->d_dres, nrd) || !f->alloc(&f->d_dsyn, nper) ||
+      !f->alloc(&f->d_Ef, ne) || !f->alloc(&f->d_Ea, ne) || !f->alloc(&f->d_bm, bm.size()) ||
+      !f->alloc(&f->d_mm, mm.size()) || !f->alloc(&f->d_nrec, P->nshot) ||
+      !f->alloc(&f->d_idx, P->npar)) {
+    set_err("emmi_fg_create: device allocation failed");
+    emmi_fg_destroy(f);
+    return EMMI_ENOMEM;
+  }
+  cudaStream_t st = f->st;
+  cudaMemcpyAsync(f->d_src, rsrc.data(), rsrc.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_rec, rrec.data(), rrec.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_delta, P->delta, nper * sizeof(float), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_dobs, P->dobs, nper * sizeof(float2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_skin, skin.data(), skin.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_bm, bm.data(), bm.size(), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_mm, mm.data(), mm.size(), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_nrec, P->nrec_shot, P->nshot * sizeof(int), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_idx, P->idxpar, P->npar * sizeof(int), cudaMemcpyHostToDevice, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_err("emmi_fg_create: %s", cudaGetErrorString(e));
+    emmi_fg_destroy(f);
+    return EMMI_ECUDA;
+  }
+  *out = f;
+  return EMMI_OK;
+}
+
+int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const float* yy,
+                 const float* zz, const float* pad, const float* rho11, const float* rho33,
+                 float* fcost, float* grad, float* phess, float* dcal, float* rmse,
+                 emmi_rhs_stats* stats) {
+  if (!f || !xx || !yy || !zz || !pad || !rho11 || !rho33 || !fcost || !grad) {
+    set_err("emmi_fg_eval: bad argument");
+    return EMMI_EINVAL;
+  }
+  // the front end: every shot's homogenization of the current model
+  int rc = emmi_homogenize_batch(nxp, nyp, nzp, xx, yy, zz, pad, f->nshot, f->n1, f->n2, f->n3,
+                                 f->x1.data(), f->x2.data(), f->x3.data(), f->d_cells, f->st);
+  if (rc != EMMI_OK) return rc;
+  emmi_problem P = {f->n1,         f->n2,        f->n3,        f->nshot,
+                    f->nrhs,       f->x1.data(), f->x2.data(), f->x3.data(),
+                    f->d_cells,    f->op.data(), f->omega_rhs.data(), f->rho_water_op.data()};
+  emmi_solver* s = nullptr;
+  rc = emmi_solver_create_dc(&s, &P, &f->opt);
+  if (rc != EMMI_OK) return rc;
+  const cudaStream_t st = s->st;
+  const long S = s->hier[0][0].S;
+  std::vector<emmi_rhs_stats> tmp;
+  emmi_rhs_stats* sf = stats;
+  if (!sf) {
+    tmp.resize(2 * (size_t)f->nrhs);
+    sf = tmp.data();
+  }
+  auto volume = [&](float2* out) {
+    for (int r = 0; r < f->nrhs; r++) {
+      SGrid G = sgrid_of(s);
+      const int o = f->op[r];
+      G.g = s->sgeo + (long)o * s->gstride;
+      k_extract_volume<<<nblk(f->nxyz), 256, 0, st>>>(
+          G, 0, f->nx, f->ny, f->nz, f->o[0], f->o[1], f->o[2], f->d[0], f->d[1], f->d[2],
+          f->d_rho33, s->raw_cells + ((long)o * 4 + 2) * f->nc, s->u64[0] + (long)r * 3 * S,
+          out + (long)r * f->nxyz, (long)f->nrhs * f->nxyz);
+    }
+  };
+  double* E = (double*)s->u64[0];
+  double* H = (double*)s->f64[0];
+  cudaMemcpyAsync(f->d_rho11, rho11, f->nxyz * sizeof(float), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_rho33, rho33, f->nxyz * sizeof(float), cudaMemcpyHostToDevice, st);
+  // 1. forward modelling of every shot and frequency
+  rc = emmi_inject_sources_dev(s, f->d_src, f->nsrc_ch, f->src_ch.data(), E);
+  if (rc == EMMI_OK) rc = emmi_solver_solve_resident(s, nullptr, nullptr, sf);
+  if (rc == EMMI_OK)
+    rc = emmi_extract_receivers_dev(s, f->d_rec, f->nrec, f->nch, f->rec_ch.data(), E, H,
+                                    (float*)f->d_dcal);
+  if (rc == EMMI_OK) {
+    volume(f->d_Ef);
+    // 2. misfit and adjoint sources
+    k_misfit<<<f->nshot, 256, 0, st>>>(f->nch, f->nfreq, f->nrec, f->d_nrec, f->d_skin, f->d_src,
+                                       f->d_rec, f->d_dobs, f->d_delta, f->d_dcal, f->d_dres,
+                                       f->d_rmse, f->d_dsyn, f->d_term, f->d_fcost);
+    // 3. adjoint modelling (H's buffer is the scratch of the magnetic part)
+    rc = emmi_inject_adjoint_dev(s, f->d_rec, f->nrec, f->nch, f->rec_ch.data(),
+                                 (const float*)f->d_dres, E, H);
+  }
+  if (rc == EMMI_OK) rc = emmi_solver_solve_resident(s, nullptr, nullptr, sf + f->nrhs);
+  if (rc == EMMI_OK) {
+    volume(f->d_Ea);
+    // 4. the gradient, summed over shots and frequencies
+    const long ne = (long)f->nrhs * f->nxyz;
+    k_gradient<<<nblk(f->nxyz), 256, 0, st>>>(
+        (int)f->nxyz, f->nshot, f->nfreq, f->npar, f->d_idx, f->preco, f->d[0] * f->d[1] * f->d[2],
+        f->d_Ef, f->d_Ef + ne, f->d_Ef + 2 * ne, f->d_Ea, f->d_Ea + ne, f->d_Ea + 2 * ne,
+        f->d_rho11, f->d_rho33, f->d_mm, f->d_bm, f->d_grad, f->d_phess);
+    const size_t nper = (size_t)f->nshot * f->nch * f->nfreq * f->nrec;
+    cudaMemcpyAsync(fcost, f->d_fcost, f->nshot * sizeof(float), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(grad, f->d_grad, f->npar * f->nxyz * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (phess && f->preco == 1)
+      cudaMemcpyAsync(phess, f->d_phess, f->npar * f->nxyz * sizeof(float),
+                      cudaMemcpyDeviceToHost, st);
+    if (dcal) cudaMemcpyAsync(dcal, f->d_dsyn, nper * sizeof(float2), cudaMemcpyDeviceToHost, st);
+    if (rmse) cudaMemcpyAsync(rmse, f->d_rmse, nper * sizeof(float), cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    const cudaError_t e2 = cudaGetLastError();
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      set_err("emmi_fg_eval: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+      rc = EMMI_ECUDA;
+    }
+  }
+  emmi_solver_destroy(s);
+  return rc;
+}
+
+int emmi_misfit_batch(int nshot, int nch, int nfreq, int nrec, const int* nrec_shot,
+                      const float* omega, float rho_water, const float* src, const float* rec,
+                      const float* dobs, const float* delta, const float* dcal, float* dres,
+                      float* rmse, float* fcost) {
+  if (nshot < 1 || nch < 1 || nfreq < 1 || nrec < 1 || !nrec_shot || !omega || !src || !rec ||
+      !dobs || !delta || !dcal || !dres || !rmse || !fcost) {
+    set_err("emmi_misfit_batch: bad argument");
+    return EMMI_EINVAL;
+  }
+  for (int k = 0; k < nshot; k++)
+    if (nrec_shot[k] < 0 || nrec_shot[k] > nrec) {
+      set_err("emmi_misfit_batch: bad receiver count");
+      return EMMI_EINVAL;
+    }
+  const size_t nper = (size_t)nshot * nch * nfreq * nrec;
+  std::vector<float> skin(nfreq), rsrc, rrec;
+  for (int k = 0; k < nfreq; k++) skin[k] = misfit_skin(omega[k], rho_water);
+  per_rhs_points(nshot, nfreq, nrec, nrec_shot, src, rec, rsrc, rrec);
+  // dcal from the per-shot layout [shot][c][f][ir] to the per-RHS one
+  // [shot * nfreq + f][c][ir] that receiver extraction writes
+  std::vector<float2> rcal(nper), rres(nper);
+  auto rhs_index = [&](int sh, int c, int f, int ir) {
+    return (((size_t)sh * nfreq + f) * nch + c) * nrec + ir;
+  };
+  for (int sh = 0; sh < nshot; sh++)
+    for (int c = 0; c < nch; c++)
+      for (int f = 0; f < nfreq; f++)
+        for (int ir = 0; ir < nrec; ir++) {
+          const size_t q = (((size_t)sh * nch + c) * nfreq + f) * nrec + ir;
+          rcal[rhs_index(sh, c, f, ir)] = make_float2(dcal[2 * q], dcal[2 * q + 1]);
+        }
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  std::vector<void*> bufs;
+  auto dev = [&](size_t bytes, const void* from) -> void* {
+    void* p = nullptr;
+    if (cudaMallocAsync(&p, bytes + 16, st) != cudaSuccess) return nullptr;
+    bufs.push_back(p);
+    if (from) cudaMemcpyAsync(p, from, bytes, cudaMemcpyHostToDevice, st);
+    return p;
+  };
+  float* d_skin = (float*)dev(nfreq * sizeof(float), skin.data());
+  float* d_src = (float*)dev(rsrc.size() * sizeof(float), rsrc.data());
+  float* d_rec = (float*)dev(rrec.size() * sizeof(float), rrec.data());
+  float2* d_dobs = (float2*)dev(nper * sizeof(float2), dobs);
+  float* d_delta = (float*)dev(nper * sizeof(float), delta);
+  float2* d_dcal = (float2*)dev(nper * sizeof(float2), rcal.data());
+  float2* d_dres = (float2*)dev(nper * sizeof(float2), nullptr);
+  float* d_rmse = (float*)dev(nper * sizeof(float), nullptr);
+  float2* d_dsyn = (float2*)dev(nper * sizeof(float2), nullptr);
+  double* d_term = (double*)dev(nper * sizeof(double), nullptr);
+  float* d_fcost = (float*)dev(nshot * sizeof(float), nullptr);
+  int* d_nrec = (int*)dev(nshot * sizeof(int), nrec_shot);
+  int rc = EMMI_OK;
+  if (bufs.size() != 12) {
+    set_err("emmi_misfit_batch: device allocation failed");
+    rc = EMMI_ENOMEM;
+  } else {
+    k_misfit<<<nshot, 256, 0, st>>>(nch, nfreq, nrec, d_nrec, d_skin, d_src, d_rec, d_dobs,
+                                    d_delta, d_dcal, d_dres, d_rmse, d_dsyn, d_term, d_fcost);
+    cudaMemcpyAsync(rres.data(), d_dres, nper * sizeof(float2), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(rmse, d_rmse, nper * sizeof(float), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(fcost, d_fcost, nshot * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+      set_err("emmi_misfit_batch: CUDA failure");
+      rc = EMMI_ECUDA;
+    }
+  }
+  for (void* p : bufs) cudaFreeAsync(p, st);
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (rc == EMMI_OK)
+    for (int sh = 0; sh < nshot; sh++)
+      for (int c = 0; c < nch; c++)
+        for (int f = 0; f < nfreq; f++)
+          for (int ir = 0; ir < nrec; ir++) {
+            const size_t q = (((size_t)sh * nch + c) * nfreq + f) * nrec + ir;
+            const float2 v = rres[rhs_index(sh, c, f, ir)];
+            dres[2 * q] = v.x;
+            dres[2 * q + 1] = v.y;
+          }
   return rc;
 }
 

@@ -406,3 +406,26 @@ def build_gradient(nxyz, o, d, idxpar, preco, Ef, Ea, rho11, rho33, bathy, src, 
                                      _p(rec), C.c_float(drmute), _p(grad), _p(phess)),
            "emmi_build_gradient")
     return grad, phess
+
+
+def misfit_batch(dobs, dcal, delta, omegas, rho_water, src, rec, nrec_shot):
+    """The device data misfit (emmi_misfit_batch): dobs, dcal complex64 and
+    delta float32 [nshot, nch, nfreq, nrec]; src [nshot, 5]; rec
+    [nshot, nrec, 5]; nrec_shot [nshot] receivers of each shot.  Returns
+    (fcost [nshot], dres complex64, rmse float32), dres and rmse shaped like
+    dobs."""
+    dobs = np.ascontiguousarray(dobs, np.complex64)
+    dcal = np.ascontiguousarray(dcal, np.complex64)
+    delta = np.ascontiguousarray(delta, np.float32)
+    nshot, nch, nfreq, nrec = dobs.shape
+    om = np.ascontiguousarray(omegas, np.float32)
+    src = np.ascontiguousarray(src, np.float32).reshape(nshot, 5)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(nshot, nrec, 5)
+    nrs = np.ascontiguousarray(nrec_shot, np.int32)
+    dres = np.zeros_like(dobs)
+    rmse = np.zeros(dobs.shape, np.float32)
+    fcost = np.zeros(nshot, np.float32)
+    _check(lib().emmi_misfit_batch(nshot, nch, nfreq, nrec, _p(nrs), _p(om), C.c_float(rho_water),
+                                   _p(src), _p(rec), _p(dobs), _p(delta), _p(dcal), _p(dres),
+                                   _p(rmse), _p(fcost)), "emmi_misfit_batch")
+    return fcost, dres, rmse

@@ -47,12 +47,15 @@ def test_emmi_main_matches_reference_output(golden, tmp_path, prec):
 
 
 @gpu
+@pytest.mark.parametrize("batch", [0, 1])
 @pytest.mark.parametrize("prec,tol", [(0, "1e-10"), (1, "1e-9")])
-def test_emmi_main_gradient_matches_reference(golden, tmp_path, prec, tol):
+def test_emmi_main_gradient_matches_reference(golden, tmp_path, prec, tol, batch):
     """mode=2 (one data gradient, src/fg_fwi.c) on the 16^3 layered case:
     observed data from the reference's mode=0 run on the true model, the
     gradient of the start model, against the reference's gradient files
-    (within 1e-3 of the largest value, and in the L2 norm)."""
+    (within 1e-3 of the largest value, and in the L2 norm); batch=1 is the
+    device evaluation of every shot at once, batch=0 the drop-in entry
+    points shot by shot."""
     import dataclasses
     g = golden("tiny_grad")
     true = W.tiny_layered()
@@ -62,7 +65,7 @@ def test_emmi_main_gradient_matches_reference(golden, tmp_path, prec, tol):
     (tmp_path / "emf_0001.txt").write_text(str(g["obs_text"]))
     args = [a for a in start.params(str(tmp_path)) if not a.startswith(("mode=", "verb="))]
     args += ["mode=2", "verb=1", "addnoise=0", "npar=2", "idxpar=1,2", "preco=1",
-             f"tol={tol}", "ncycle=120", f"gmg_precision={prec}"]
+             f"tol={tol}", "ncycle=120", f"gmg_precision={prec}", f"batch={batch}"]
     r = subprocess.run([MAIN] + args, cwd=tmp_path, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     for nm in ("grad_Rv", "grad_Rh"):
@@ -108,8 +111,9 @@ def _trace(stdout):
 
 
 @gpu
+@pytest.mark.parametrize("batch", [0, 1])
 @pytest.mark.parametrize("prec,tol", [(0, "1e-10"), (1, "1e-9")])
-def test_emmi_main_inversion_matches_reference(golden, tmp_path, prec, tol):
+def test_emmi_main_inversion_matches_reference(golden, tmp_path, prec, tol, batch):
     """mode=1 (the l-BFGS inversion, src/do_fwi.c) for two iterations on the
     layered case (21 x 21 x 11 cells) from the start model, against the
     reference's own run.
@@ -139,7 +143,7 @@ def test_emmi_main_inversion_matches_reference(golden, tmp_path, prec, tol):
     (tmp_path / "emf_0001.txt").write_text(str(g["obs_text"]))
     args = [a for a in start.params(str(tmp_path)) if not a.startswith(("mode=", "verb="))]
     args += ["mode=1", "verb=1", "addnoise=0", "npar=2", "idxpar=1,2", "preco=1", "niter=2",
-             f"tol={tol}", "ncycle=120", f"gmg_precision={prec}"]
+             f"tol={tol}", "ncycle=120", f"gmg_precision={prec}", f"batch={batch}"]
     r = subprocess.run([MAIN] + args, cwd=tmp_path, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr
     ours = _iterate_rows(open(tmp_path / "iterate.txt").read())
@@ -178,3 +182,73 @@ def test_emmi_main_inversion_matches_reference(golden, tmp_path, prec, tol):
     for nm in ("Rv", "Rh"):
         o = np.fromfile(tmp_path / f"{nm}_iteration_01", np.float32)
         assert np.isfinite(o).all() and (o > 0).all()
+
+
+def _ragged_three_shots():
+    """The layered case with three sources, two frequencies and a different
+    receiver set per shot (all 21, the first 15, every other one)."""
+    import dataclasses
+    s = W.tiny_layered()
+    src = np.array([[-1000.0, 0.0, 950.0, 0.0, 0.0], [0.0, 500.0, 950.0, 30.0, 0.0],
+                    [1500.0, -500.0, 950.0, -20.0, 0.0]], np.float32)
+    nrec = len(s.receivers)
+    pairs = [(1, r) for r in range(1, nrec + 1)] + [(2, r) for r in range(1, 16)] + \
+            [(3, r) for r in range(1, nrec + 1, 2)]
+    return dataclasses.replace(s, sources=src, pairs=np.array(pairs), freqs=[0.5, 1.0])
+
+
+
+@gpu
+@pytest.mark.parametrize("preco", [1, 0])
+def test_batched_evaluation_matches_shot_by_shot(tmp_path, preco):
+    """mode=2 over three shots with ragged receiver sets and two frequencies:
+    the device evaluation of every shot and frequency at once (batch=1)
+    against the drop-in entry points shot by shot (batch=0), both FP64 to
+    1e-10: gradients, pseudo-Hessian, misfits, synthetic data and rmse
+    files."""
+    import dataclasses
+    true = _ragged_three_shots()
+    tdir = tmp_path / "true"
+    true.write(str(tdir))
+    args = [a for a in true.params(str(tdir)) if not a.startswith("shots=")]
+    r = subprocess.run([MAIN] + args + ["shots=1,2,3", "tol=1e-10", "ncycle=120",
+                                        "gmg_precision=0"],
+                       cwd=tdir, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rho = true.rho11.copy()
+    rho[rho == 100.0] = 1.0  # the start model: no resistive layer
+    start = dataclasses.replace(true, rho11=rho, rho22=rho.copy(), rho33=rho.copy())
+    out = {}
+    for batch in (0, 1):
+        d = tmp_path / f"b{batch}"
+        start.write(str(d))
+        for k in (1, 2, 3):
+            (d / f"emf_{k:04d}.txt").write_text((tdir / f"emf_{k:04d}.txt").read_text())
+        a = [x for x in start.params(str(d)) if not x.startswith(("mode=", "verb=", "shots="))]
+        a += ["mode=2", "verb=1", "shots=1,2,3", "addnoise=0", "npar=2", "idxpar=1,2",
+              f"preco={preco}", "tol=1e-10", "ncycle=120", "gmg_precision=0", f"batch={batch}"]
+        r = subprocess.run([MAIN] + a, cwd=d, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout[-3000:] + r.stderr
+        o = {nm: np.fromfile(d / nm, np.float32)
+             for nm in ("gradient_dat_Rv", "gradient_dat_Rh")}
+        if preco == 1:
+            o["gradient_phess"] = np.fromfile(d / "gradient_phess", np.float32)
+        o["fcost"] = [float(l.split("fcost=")[1].split(",")[0]) for l in r.stdout.splitlines()
+                      if l.startswith("isrc=")]
+        for k in (1, 2, 3):
+            o[f"syn{k}"] = read_emf(d / f"syn_{k:04d}.txt")
+            o[f"rmse{k}"] = np.loadtxt(d / f"rmse_{k:04d}.txt", skiprows=1, usecols=(4,))
+        out[batch] = o
+    a, b = out[0], out[1]
+    assert len(a["fcost"]) == len(b["fcost"]) == 3
+    np.testing.assert_allclose(b["fcost"], a["fcost"], rtol=1e-5)
+    for nm in [k for k in a if k.startswith("gradient")]:
+        err = np.abs(b[nm] - a[nm]).max() / np.abs(a[nm]).max()
+        print(nm, f"max {err:.2e}")
+        assert err < 1e-5, (nm, err)
+    for k in (1, 2, 3):
+        for ch in a[f"syn{k}"]:
+            x, y = a[f"syn{k}"][ch], b[f"syn{k}"][ch]
+            assert x.shape == y.shape and np.abs(y - x).max() <= 1e-5 * np.abs(x).max(), (k, ch)
+        np.testing.assert_allclose(b[f"rmse{k}"], a[f"rmse{k}"], rtol=1e-5, atol=1e-6)
+    assert [len(a[f"rmse{k}"]) for k in (1, 2, 3)] == [2 * 4 * 21, 2 * 4 * 15, 2 * 4 * 11]
