@@ -21,6 +21,12 @@ channels -- as one batch: inject the 25 sources, solve all 25 systems to
   cpu_baseline the CPU restatement of the reference's algorithm on the host
          cores, one F-cycle per thread as a bounded sample, scaled by the
          cycles a solve takes
+  fwi_eval     one objective evaluation of the inversion (the reference's
+         fg_fwi) on the gradient configuration -- 25 shots x 3 frequencies
+         (0.25, 0.5, 1 Hz) at 128^3, the gradient of the half-space start
+         model against the reservoir model's data -- through the C ABI
+         (emmi_fg_eval) from host arrays: 75 forward and 75 adjoint solves,
+         misfit, adjoint sources and the shot-summed gradient
 
   python bench.py [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank solves its own copy of the batch (weak scaling).
@@ -57,6 +63,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fwi", action="store_true",
+                   help="skip the inversion objective evaluation (fwi_eval)")
     p.add_argument("--nrhs", type=int, default=0, help="use only the first k shots")
     p.add_argument("--no-learned", action="store_true",
                    help="plain complex64 cycles (no learned correction)")
@@ -124,6 +132,44 @@ def build_workload(n: int):
     return dict(survey=s, X1=X1, X2=X2, X3=X3, cells=cells, omega=np.full(len(src), om, np.float32),
                 rho_water=np.float32(m.rho_water()), src=srcr, rec=rec, grids=grids, model=m,
                 src_xyz=src[:, :3].copy())
+
+
+def fwi_eval_bench(n: int, tol: float):
+    """Seconds per inversion objective evaluation (fg_fwi) of the gradient
+    configuration, host arrays in and out through emmi_fg_eval.  The
+    observed data are the reservoir model's own synthetic data (one
+    evaluation with zero data), uncertainties 3% of the amplitude plus a
+    floor; the timed evaluation is the second one at the start model."""
+    from libemmi_mgfd_gb300 import gpu as G
+    from libemmi_mgfd_gb300 import host
+    from libemmi_mgfd_gb300 import workloads as W
+    true = W.config4(n, true_model=True)
+    start = W.config4(n, true_model=False)
+    mt, ms = host.Model.from_survey(true), host.Model.from_survey(start)
+    nshot, nch, nf = len(true.sources), len(true.chrec), len(true.freqs)
+    nrec = int(np.bincount(np.asarray(true.pairs)[:, 0]).max())
+    opts = G.Options(precision=G.PREC_MIXED, tol=tol, ncycle=100)
+    shape = (nshot, nch, nf, nrec)
+    f = G.Fg(mt, true, np.zeros(shape, np.complex64), np.ones(shape, np.float32), true.bathy,
+             options=opts)
+    dobs = f.eval(mt)[3]
+    f.close()
+    delta = (0.03 * np.abs(dobs) + 1e-15).astype(np.float32)
+    f = G.Fg(ms, start, dobs, delta, start.bathy, options=opts)
+    f.eval(ms)
+    t0 = time.perf_counter()
+    fcost, grad, phess, dcal, rmse, cyc = f.eval(ms)
+    dt = time.perf_counter() - t0
+    out = {"seconds_per_evaluation": round(dt, 3), "shots": nshot, "freqs": nf,
+           "solves": 2 * nshot * nf, "solves_per_s": round(2 * nshot * nf / dt, 2),
+           "cycles_mean_forward": float(cyc[0].mean()), "cycles_mean_adjoint": float(cyc[1].mean()),
+           "fcost": float(fcost.astype(np.float64).sum()),
+           "grad_finite": bool(np.isfinite(grad).all() and np.abs(grad).max() > 0),
+           "h2d_bytes": int(f.h2d_bytes), "d2h_bytes": int(f.d2h_bytes),
+           "workload": f"c4_reservoir_{n}^3_25shots_3freqs, gradient at the half-space start "
+                       "model, mixed precision to tol", "tol": tol}
+    f.close()
+    return out
 
 
 def make_solver(w, precision, tol, krylov=0):
@@ -450,6 +496,10 @@ def main():
         cpu = {"value": round(v, 5), "unit": UNIT, "cores": nthr, "kind": "port",
                "sample": sample}
 
+    fwi = None
+    if rank == 0 and not a.no_fwi:
+        fwi = fwi_eval_bench(a.n, a.tol)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
@@ -470,7 +520,7 @@ def main():
             "learned": learned, "mixed_without_learned": without,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": round(value / plain["value"], 3) if plain else None,
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fwi_eval": fwi,
             "gpu_launches": timed_launches, "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -429,3 +429,108 @@ def misfit_batch(dobs, dcal, delta, omegas, rho_water, src, rec, nrec_shot):
                                    _p(src), _p(rec), _p(dobs), _p(delta), _p(dcal), _p(dres),
                                    _p(rmse), _p(fcost)), "emmi_misfit_batch")
     return fcost, dres, rmse
+
+
+class _FgProblem(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("o", C.c_float * 3),
+                ("d", C.c_float * 3), ("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int),
+                ("nshot", C.c_int), ("nfreq", C.c_int), ("omega", C.c_void_p),
+                ("x1", C.c_void_p), ("x2", C.c_void_p), ("x3", C.c_void_p),
+                ("rho_water", C.c_float), ("nsrc_ch", C.c_int), ("src_ch", C.c_void_p),
+                ("nrec_ch", C.c_int), ("rec_ch", C.c_void_p), ("nrec", C.c_int),
+                ("nrec_shot", C.c_void_p), ("src", C.c_void_p), ("rec", C.c_void_p),
+                ("dobs", C.c_void_p), ("delta", C.c_void_p), ("npar", C.c_int),
+                ("idxpar", C.c_void_p), ("preco", C.c_int), ("bathy", C.c_void_p),
+                ("dsmute", C.c_float), ("drmute", C.c_float)]
+
+
+class Fg:
+    """The inversion's objective evaluation for a batch of shots on the
+    device (emmi_fg_create / emmi_fg_eval): forward solves, misfit, adjoint
+    solves and the shot-summed gradient in one pass.
+
+    model: host.Model (geometry and start resistivities); survey: its
+    Survey (sources, receivers, pairs, channels, frequencies); dobs complex64
+    and delta float32 [nshot, nrec_ch, nfreq, nrec]; bathy [ny, nx]."""
+
+    def __init__(self, model, survey, dobs, delta, bathy, options: Optional[Options] = None,
+                 idxpar=(1, 2), preco: int = 1, dsmute: float = 800.0, drmute: float = 200.0):
+        opts = (options or Options())._c()
+        xx, yy, zz, _ = model.padded()
+        src = np.asarray(survey.sources, np.float32).copy()
+        src[:, 3:] = np.deg2rad(src[:, 3:])
+        nshot = len(src)
+        recs = [np.asarray(survey.pairs)[np.asarray(survey.pairs)[:, 0] == k + 1, 1] - 1
+                for k in range(nshot)]
+        nrec = max(1, max(len(r) for r in recs))
+        rec = np.zeros((nshot, nrec, 5), np.float32)
+        allrec = np.asarray(survey.receivers, np.float32).copy()
+        allrec[:, 3:] = np.deg2rad(allrec[:, 3:])
+        for k, r in enumerate(recs):
+            rec[k, :len(r)] = allrec[r]
+        ax = [model.axes(xx, yy, zz, float(p[0]), float(p[1]), float(p[2])) for p in src]
+        self.nshot, self.nrec, self.npar, self.preco = nshot, nrec, len(idxpar), preco
+        self.nch, self.nfreq = len(survey.chrec), len(survey.freqs)
+        self.nxyz = (model.nz, model.ny, model.nx)
+        keep = dict(
+            omega=(2 * np.pi * np.asarray(survey.freqs, np.float64)).astype(np.float32),
+            x1=np.stack([a["x1"] for a in ax]), x2=np.stack([a["x2"] for a in ax]),
+            x3=np.stack([a["x3"] for a in ax]),
+            src_ch=np.array([CHANNELS[c] for c in survey.chsrc], np.int32),
+            rec_ch=np.array([CHANNELS[c] for c in survey.chrec], np.int32),
+            nrec_shot=np.array([len(r) for r in recs], np.int32), src=src, rec=rec,
+            dobs=np.ascontiguousarray(dobs, np.complex64).reshape(nshot, self.nch, self.nfreq,
+                                                                    nrec),
+            delta=np.ascontiguousarray(delta, np.float32).reshape(nshot, self.nch, self.nfreq,
+                                                                  nrec),
+            idxpar=np.array(idxpar, np.int32), bathy=np.ascontiguousarray(bathy, np.float32))
+        P = _FgProblem(model.nx, model.ny, model.nz, (C.c_float * 3)(model.ox, model.oy, model.oz),
+                       (C.c_float * 3)(model.dx, model.dy, model.dz), model.n1, model.n2,
+                       model.n3, nshot, self.nfreq, _p(keep["omega"]), _p(keep["x1"]),
+                       _p(keep["x2"]), _p(keep["x3"]), model.rho_water(), len(keep["src_ch"]),
+                       _p(keep["src_ch"]), self.nch, _p(keep["rec_ch"]), nrec,
+                       _p(keep["nrec_shot"]), _p(src), _p(rec), _p(keep["dobs"]),
+                       _p(keep["delta"]), self.npar, _p(keep["idxpar"]), preco,
+                       _p(keep["bathy"]), dsmute, drmute)
+        h = C.c_void_p()
+        _check(lib().emmi_fg_create(C.byref(h), C.byref(P), C.byref(opts)), "emmi_fg_create")
+        self._h = h
+        self._keep = keep
+        # host -> device bytes of one evaluation: padded model + two grids
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
+
+    def eval(self, model):
+        """(fcost [nshot], grad, phess [npar, nz, ny, nx], dcal complex64 and
+        rmse [nshot, nch, nfreq, nrec], stats [2, nshot * nfreq] (cycles))
+        at the resistivities of model (host.Model on the same grid)."""
+        xx, yy, zz, pad = model.padded()
+        r11 = np.ascontiguousarray(model.rho11, np.float32)
+        r33 = np.ascontiguousarray(model.rho33, np.float32)
+        nz, ny, nx = self.nxyz
+        fcost = np.zeros(self.nshot, np.float32)
+        grad = np.zeros((self.npar, nz, ny, nx), np.float32)
+        phess = np.zeros_like(grad)
+        shp = (self.nshot, self.nch, self.nfreq, self.nrec)
+        dcal = np.zeros(shp, np.complex64)
+        rmse = np.zeros(shp, np.float32)
+        stats = (_Stats * (2 * self.nshot * self.nfreq))()
+        _check(lib().emmi_fg_eval(self._h, len(xx) - 1, len(yy) - 1, len(zz) - 1, _p(xx), _p(yy),
+                                  _p(zz), _p(pad), _p(r11), _p(r33), _p(fcost), _p(grad),
+                                  _p(phess), _p(dcal), _p(rmse), stats), "emmi_fg_eval")
+        self.h2d_bytes = sum(a.nbytes for a in (xx, yy, zz, pad, r11, r33))
+        self.d2h_bytes = sum(a.nbytes for a in (fcost, grad, dcal, rmse)) + \
+            (phess.nbytes if self.preco == 1 else 0)
+        cyc = np.array([s.cycles for s in stats]).reshape(2, -1)
+        return fcost, grad, phess, dcal, rmse, cyc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().emmi_fg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
