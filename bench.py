@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fwi", action="store_true",
                    help="skip the inversion objective evaluation (fwi_eval)")
+    p.add_argument("--only-fwi", action="store_true",
+                   help="run only the inversion objective evaluation and print it")
     p.add_argument("--nrhs", type=int, default=0, help="use only the first k shots")
     p.add_argument("--no-learned", action="store_true",
                    help="plain complex64 cycles (no learned correction)")
@@ -166,6 +168,7 @@ def fwi_eval_bench(n: int, tol: float):
            "fcost": float(fcost.astype(np.float64).sum()),
            "grad_finite": bool(np.isfinite(grad).all() and np.abs(grad).max() > 0),
            "h2d_bytes": int(f.h2d_bytes), "d2h_bytes": int(f.d2h_bytes),
+           "phases_ms": f.phases_ms,
            "workload": f"c4_reservoir_{n}^3_25shots_3freqs, gradient at the half-space start "
                        "model, mixed precision to tol", "tol": tol}
     f.close()
@@ -303,6 +306,10 @@ def main():
     from libemmi_mgfd_gb300 import gpu as G
     B.build()
     torch.cuda.set_device(local)
+    if a.only_fwi:
+        if rank == 0:
+            print(json.dumps({"fwi_eval": fwi_eval_bench(a.n, a.tol)}), flush=True)
+        return
     w = build_workload(a.n)
     s = w["survey"]
     if a.nrhs > 0 or a.profile:

@@ -307,6 +307,12 @@ int emmi_fg_eval(emmi_fg *f, int nxp, int nyp, int nzp, const float *xx,
                  const float *rho11, const float *rho33, float *fcost,
                  float *grad, float *phess, float *dcal, float *rmse,
                  emmi_rhs_stats *stats);
+/* milliseconds of the last evaluation's phases: [0] front end
+ * (homogenization), [1] solver set-up (host clock), [2] forward solves,
+ * [3] receiver data and forward fields on the model grid, [4] misfit,
+ * [5] adjoint sources, [6] adjoint solves, [7] adjoint fields, gradient and
+ * copies out (CUDA events on the solver's stream) */
+int emmi_fg_phases(const emmi_fg *f, double ms[8]);
 void emmi_fg_destroy(emmi_fg *f);
 /* The device misfit alone on host arrays (parity checks): per-shot arrays
  * dobs, dcal, dres (complex, interleaved), delta, rmse [nshot][nch][nfreq]

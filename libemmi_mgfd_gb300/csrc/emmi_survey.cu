@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -166,43 +167,65 @@ __global__ void k_inject_sources(SGrid G0, int gstride, const int* __restrict__ 
   }
 }
 
-// adjoint sources, one thread per RHS over its receivers in order; b and m
-// zeroed beforehand (inject_extract.c:124-301)
-__global__ void k_inject_adjoint(SGrid G0, int gstride, const int* __restrict__ op,
-                                 const float* __restrict__ rec, int nrec,
-                                 const float* __restrict__ omega, ChanList chs,
-                                 const float2* __restrict__ dres, double2* __restrict__ b,
-                                 double2* __restrict__ m, int nrhs) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrhs) return;
+// one adjoint-source term: a trilinear stencil on one staggered grid and
+// the value it spreads
+struct AdjTerm {
+  Tri t;
+  double2 v;
+};
+
+// adjoint-source terms (inject_extract.c:124-301), one thread per (RHS,
+// receiver): for each component c the electric term i*omega*mu0*F[c]/vol
+// on E's grid (terms 0..2) and the magnetic term M[c]/vol on H's grid
+// (terms 3..5), F and M the receiver-frame residuals rotated to the grid
+__global__ void k_adjoint_terms(SGrid G0, int gstride, const int* __restrict__ op,
+                                const float* __restrict__ rec, int nrec,
+                                const float* __restrict__ omega, ChanList chs,
+                                const float2* __restrict__ dres, AdjTerm* __restrict__ terms,
+                                int nrhs) {
+  const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (id >= (long)nrhs * nrec) return;
+  const int r = (int)(id / nrec), ir = (int)(id % nrec);
   SGrid G = G0;
   G.g = G0.g + (long)op[r] * gstride;
-  const long S = (long)(G.n[0] + 1) * (G.n[1] + 1) * (G.n[2] + 1);
-  double2* yb = b + (long)r * 3 * S;
-  double2* ym = m + (long)r * 3 * S;
   const zd iw = {0.0 * kMu0, (double)omega[r] * kMu0};
+  const float* p = rec + ((long)r * nrec + ir) * 5;
+  zd F[3] = {{0, 0}, {0, 0}, {0, 0}}, M[3] = {{0, 0}, {0, 0}, {0, 0}};
+  for (int ic = 0; ic < chs.n; ic++) {
+    const float2 d = dres[((long)r * chs.n + ic) * nrec + ir];
+    if (chs.ch[ic] <= 2) rotate_in(chs.ch[ic], p[3], p[4], zd{(double)d.x, (double)d.y}, F);
+  }
+  for (int ic = 0; ic < chs.n; ic++) {
+    const float2 d = dres[((long)r * chs.n + ic) * nrec + ir];
+    if (chs.ch[ic] >= 3) rotate_in(chs.ch[ic] - 3, p[3], p[4], zd{(double)d.x, (double)d.y}, M);
+  }
+  AdjTerm* out = terms + id * 6;
+  for (int c = 0; c < 3; c++) {
+    const Tri t = trilin(G, c == 0, c == 1, c == 2, p[0], p[1], p[2]);
+    const zd v = zdiv_real(zmul(iw, F[c]), (double)t.vol);
+    out[c] = AdjTerm{t, make_double2(v.re, v.im)};
+  }
+  for (int c = 0; c < 3; c++) {
+    const Tri t = trilin(G, c != 0, c != 1, c != 2, p[0], p[1], p[2]);
+    const zd v = zdiv_real(M[c], (double)t.vol);
+    out[3 + c] = AdjTerm{t, make_double2(v.re, v.im)};
+  }
+}
+
+// the adjoint-source terms spread in receiver order, one thread per (RHS,
+// field, component): the slots of different components are disjoint, so
+// every slot receives its additions in the reference's order; b and m
+// zeroed beforehand
+__global__ void k_adjoint_scatter(SGrid G0, const AdjTerm* __restrict__ terms, int nrec,
+                                  double2* __restrict__ b, double2* __restrict__ m, int nrhs) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nrhs * 6) return;
+  const int r = id / 6, q = id % 6, c = q % 3;
+  const long S = (long)(G0.n[0] + 1) * (G0.n[1] + 1) * (G0.n[2] + 1);
+  double2* y = (q < 3 ? b : m) + (long)r * 3 * S;
   for (int ir = 0; ir < nrec; ir++) {
-    const float* p = rec + ((long)r * nrec + ir) * 5;
-    zd F[3] = {{0, 0}, {0, 0}, {0, 0}};
-    for (int ic = 0; ic < chs.n; ic++)
-      if (chs.ch[ic] <= 2) {
-        const float2 d = dres[((long)r * chs.n + ic) * nrec + ir];
-        rotate_in(chs.ch[ic], p[3], p[4], zd{(double)d.x, (double)d.y}, F);
-      }
-    for (int c = 0; c < 3; c++) {
-      const Tri t = trilin(G, c == 0, c == 1, c == 2, p[0], p[1], p[2]);
-      scatter8(G.n, c, t, zdiv_real(zmul(iw, F[c]), (double)t.vol), yb);
-    }
-    zd M[3] = {{0, 0}, {0, 0}, {0, 0}};
-    for (int ic = 0; ic < chs.n; ic++)
-      if (chs.ch[ic] >= 3) {
-        const float2 d = dres[((long)r * chs.n + ic) * nrec + ir];
-        rotate_in(chs.ch[ic] - 3, p[3], p[4], zd{(double)d.x, (double)d.y}, M);
-      }
-    for (int c = 0; c < 3; c++) {
-      const Tri t = trilin(G, c != 0, c != 1, c != 2, p[0], p[1], p[2]);
-      scatter8(G.n, c, t, zdiv_real(M[c], (double)t.vol), ym);
-    }
+    const AdjTerm a = terms[((long)r * nrec + ir) * 6 + q];
+    scatter8(G0.n, c, a.t, zd{a.v.x, a.v.y}, y);
   }
 }
 
@@ -584,9 +607,16 @@ int emmi_inject_adjoint_dev(emmi_solver* s, const float* rec_dev, int nrec, int 
   const long S = s->hier[0][0].S;
   CK(cudaMemsetAsync(b_dev, 0, (size_t)3 * S * s->nrhs * sizeof(double2), s->st));
   CK(cudaMemsetAsync(m_dev, 0, (size_t)3 * S * s->nrhs * sizeof(double2), s->st));
-  k_inject_adjoint<<<nblk(s->nrhs, 64), 64, 0, s->st>>>(
-      sgrid_of(s), s->gstride, s->d_op, rec_dev, nrec, s->d_omega, make_chans(nch, ch),
-      (const float2*)dres_dev, (double2*)b_dev, (double2*)m_dev, s->nrhs);
+  if (nrec > 0) {
+    AdjTerm* terms = nullptr;
+    CK(cudaMallocAsync((void**)&terms, (size_t)s->nrhs * nrec * 6 * sizeof(AdjTerm), s->st));
+    k_adjoint_terms<<<nblk((long)s->nrhs * nrec, 128), 128, 0, s->st>>>(
+        sgrid_of(s), s->gstride, s->d_op, rec_dev, nrec, s->d_omega, make_chans(nch, ch),
+        (const float2*)dres_dev, terms, s->nrhs);
+    k_adjoint_scatter<<<nblk((long)s->nrhs * 6, 64), 64, 0, s->st>>>(
+        sgrid_of(s), terms, nrec, (double2*)b_dev, (double2*)m_dev, s->nrhs);
+    CK(cudaFreeAsync(terms, s->st));
+  }
   dim3 g(nblk((long)s->n[0] * s->n[1] * s->n[2]), s->nrhs);
   k_curl_m<<<g, 256, 0, s->st>>>(sgrid_of(s), s->gstride, s->d_op, (const double2*)m_dev,
                                  (double2*)b_dev);
@@ -791,6 +821,10 @@ struct emmi_fg {
   float2 *d_Ef = nullptr, *d_Ea = nullptr;
   unsigned char *d_bm = nullptr, *d_mm = nullptr;
   int *d_nrec = nullptr, *d_idx = nullptr;
+  // milliseconds of the last evaluation's phases: front end, solver set-up,
+  // forward solves, receiver data + forward fields, misfit, adjoint sources,
+  // adjoint solves, adjoint fields + gradient + copies out
+  double phase_ms[8] = {};
   std::vector<void*> owned;
   template <typename T>
   bool alloc(T** p, size_t n) {
@@ -919,10 +953,13 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
     set_err("emmi_fg_eval: bad argument");
     return EMMI_EINVAL;
   }
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
   // the front end: every shot's homogenization of the current model
   int rc = emmi_homogenize_batch(nxp, nyp, nzp, xx, yy, zz, pad, f->nshot, f->n1, f->n2, f->n3,
                                  f->x1.data(), f->x2.data(), f->x3.data(), f->d_cells, f->st);
   if (rc != EMMI_OK) return rc;
+  const auto t1 = clk::now();
   emmi_problem P = {f->n1,         f->n2,        f->n3,        f->nshot,
                     f->nrhs,       f->x1.data(), f->x2.data(), f->x3.data(),
                     f->d_cells,    f->op.data(), f->omega_rhs.data(), f->rho_water_op.data()};
@@ -930,6 +967,10 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
   rc = emmi_solver_create_dc(&s, &P, &f->opt);
   if (rc != EMMI_OK) return rc;
   const cudaStream_t st = s->st;
+  cudaEvent_t ev[7] = {};
+  for (auto& e : ev) cudaEventCreate(&e);
+  cudaEventRecord(ev[0], st);
+  const auto t2 = clk::now();
   const long S = s->hier[0][0].S;
   std::vector<emmi_rhs_stats> tmp;
   emmi_rhs_stats* sf = stats;
@@ -955,20 +996,25 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
   // 1. forward modelling of every shot and frequency
   rc = emmi_inject_sources_dev(s, f->d_src, f->nsrc_ch, f->src_ch.data(), E);
   if (rc == EMMI_OK) rc = emmi_solver_solve_resident(s, nullptr, nullptr, sf);
+  cudaEventRecord(ev[1], st);
   if (rc == EMMI_OK)
     rc = emmi_extract_receivers_dev(s, f->d_rec, f->nrec, f->nch, f->rec_ch.data(), E, H,
                                     (float*)f->d_dcal);
   if (rc == EMMI_OK) {
     volume(f->d_Ef);
+    cudaEventRecord(ev[2], st);
     // 2. misfit and adjoint sources
     k_misfit<<<f->nshot, 256, 0, st>>>(f->nch, f->nfreq, f->nrec, f->d_nrec, f->d_skin, f->d_src,
                                        f->d_rec, f->d_dobs, f->d_delta, f->d_dcal, f->d_dres,
                                        f->d_rmse, f->d_dsyn, f->d_term, f->d_fcost);
+    cudaEventRecord(ev[3], st);
     // 3. adjoint modelling (H's buffer is the scratch of the magnetic part)
     rc = emmi_inject_adjoint_dev(s, f->d_rec, f->nrec, f->nch, f->rec_ch.data(),
                                  (const float*)f->d_dres, E, H);
   }
+  cudaEventRecord(ev[4], st);
   if (rc == EMMI_OK) rc = emmi_solver_solve_resident(s, nullptr, nullptr, sf + f->nrhs);
+  cudaEventRecord(ev[5], st);
   if (rc == EMMI_OK) {
     volume(f->d_Ea);
     // 4. the gradient, summed over shots and frequencies
@@ -985,6 +1031,7 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
                       cudaMemcpyDeviceToHost, st);
     if (dcal) cudaMemcpyAsync(dcal, f->d_dsyn, nper * sizeof(float2), cudaMemcpyDeviceToHost, st);
     if (rmse) cudaMemcpyAsync(rmse, f->d_rmse, nper * sizeof(float), cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ev[6], st);
     const cudaError_t e = cudaStreamSynchronize(st);
     const cudaError_t e2 = cudaGetLastError();
     if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -992,8 +1039,30 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
       rc = EMMI_ECUDA;
     }
   }
+  if (rc == EMMI_OK) {
+    auto ms = [](clk::time_point a, clk::time_point b) {
+      return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    f->phase_ms[0] = ms(t0, t1);
+    f->phase_ms[1] = ms(t1, t2);
+    for (int k = 0; k < 6; k++) {
+      float v = 0.f;
+      cudaEventElapsedTime(&v, ev[k], ev[k + 1]);
+      f->phase_ms[2 + k] = v;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
   emmi_solver_destroy(s);
   return rc;
+}
+
+int emmi_fg_phases(const emmi_fg* f, double ms[8]) {
+  if (!f || !ms) {
+    set_err("emmi_fg_phases: bad argument");
+    return EMMI_EINVAL;
+  }
+  for (int k = 0; k < 8; k++) ms[k] = f->phase_ms[k];
+  return EMMI_OK;
 }
 
 int emmi_misfit_batch(int nshot, int nch, int nfreq, int nrec, const int* nrec_shot,

@@ -522,6 +522,11 @@ class Fg:
         self.d2h_bytes = sum(a.nbytes for a in (fcost, grad, dcal, rmse)) + \
             (phess.nbytes if self.preco == 1 else 0)
         cyc = np.array([s.cycles for s in stats]).reshape(2, -1)
+        ph = (C.c_double * 8)()
+        _check(lib().emmi_fg_phases(self._h, ph), "emmi_fg_phases")
+        self.phases_ms = dict(zip(("front_end", "setup", "forward_solves", "data_fields", "misfit",
+                                   "adjoint_sources", "adjoint_solves", "gradient_out"),
+                                  [round(v, 2) for v in ph]))
         return fcost, grad, phess, dcal, rmse, cyc
 
     def close(self):
