@@ -151,7 +151,7 @@ def trace_lines(stdout):
     return [l.strip() for l in stdout.splitlines() if l.strip().startswith(keep)]
 
 
-def mode1_case(tol="1e-10", niter=2, preco=1):
+def mode1_case(tol="1e-10", niter=2, preco=1, extra=()):
     """The reference's main in mode=1 (the l-BFGS inversion, src/do_fwi.c)
     for niter iterations from the start model of mode2_case, without noise:
     iterate.txt, rmse_misfit.txt and the resistivities after every
@@ -169,14 +169,14 @@ def mode1_case(tol="1e-10", niter=2, preco=1):
     obs_text = open(os.path.join(d, "emf_0001.txt")).read()
     args = [a for a in start.params(d) if not a.startswith("mode=") and not a.startswith("verb=")]
     args += ["mode=1", "verb=1", "addnoise=0", "npar=2", "idxpar=1,2", f"preco={preco}",
-             f"niter={niter}"] + common
+             f"niter={niter}"] + list(extra) + common
     r1 = subprocess.run([REF_MAIN] + args, cwd=d, capture_output=True, text=True)
     if r1.returncode != 0:
         raise RuntimeError(r1.stdout + r1.stderr)
     n = start.nx * start.ny * start.nz
     rec = {
         "name": np.array("tiny_fwi"),
-        "params": np.array(" ".join(args[-7:])),
+        "params": np.array(" ".join(args[-7 - len(extra):])),
         "rho_start": start.rho11,
         "obs_text": np.array(obs_text),
         "iterate": np.array(open(os.path.join(d, "iterate.txt")).read()),
@@ -215,6 +215,21 @@ def main():
     only = set(sys.argv[1:])
     if only == {"sensitivity"}:
         sensitivity()
+        return
+    if only == {"tiny_fwi_variants"}:
+        # the first inversion iteration with the depth preconditioner, the
+        # triangle smoothing and the box bounds (one iteration: the second
+        # is not reproducible, see mode1_case's test)
+        out = {}
+        for tag, preco, extra in (("p2", 2, ()), ("p3", 3, ("r1=2", "r2=2", "r3=2")),
+                                  ("bound", 1, ("bound=1", "minpar=0.5,0.5",
+                                                "maxpar=3,3"))):
+            rec = mode1_case(niter=1, preco=preco, extra=extra)
+            for k, v in rec.items():
+                out[f"{tag}_{k}"] = v
+        np.savez_compressed(os.path.join(HERE, "tiny_fwi_variants.npz"), **out)
+        print("tiny_fwi_variants",
+              os.path.getsize(os.path.join(HERE, "tiny_fwi_variants.npz")) // 1024, "KB")
         return
     if only == {"tiny_fwi"}:
         rec = mode1_case()

@@ -252,3 +252,52 @@ def test_batched_evaluation_matches_shot_by_shot(tmp_path, preco):
             assert x.shape == y.shape and np.abs(y - x).max() <= 1e-5 * np.abs(x).max(), (k, ch)
         np.testing.assert_allclose(b[f"rmse{k}"], a[f"rmse{k}"], rtol=1e-5, atol=1e-6)
     assert [len(a[f"rmse{k}"]) for k in (1, 2, 3)] == [2 * 4 * 21, 2 * 4 * 15, 2 * 4 * 11]
+
+
+@gpu
+@pytest.mark.parametrize("tag", ["p2", "p3", "bound"])
+def test_emmi_main_inversion_variants_first_iteration(golden, tmp_path, tag):
+    """mode=1, one iteration, with the depth preconditioner (preco=2), the
+    triangle smoothing (preco=3, r1=r2=r3=2) and the box bounds (bound=1,
+    minpar=0.5,0.5 maxpar=3,3): the start model's and every line-search
+    evaluation's objective and Wolfe decision, iterate.txt and the
+    resistivities after the iteration against the reference's own runs
+    (FP64, the batched evaluation)."""
+    import dataclasses
+    g = {k[len(tag) + 1:]: v for k, v in golden("tiny_fwi_variants").items()
+         if k.startswith(tag + "_")}
+    true = W.tiny_layered()
+    rho = np.asarray(g["rho_start"], np.float32)
+    start = dataclasses.replace(true, rho11=rho, rho22=rho.copy(), rho33=rho.copy())
+    start.write(str(tmp_path))
+    (tmp_path / "emf_0001.txt").write_text(str(g["obs_text"]))
+    args = [a for a in start.params(str(tmp_path)) if not a.startswith(("mode=", "verb="))]
+    args += [a for a in str(g["params"]).split() if not a.startswith(("tol=", "ncycle="))]
+    args += ["mode=1", "verb=1", "tol=1e-10", "ncycle=120", "gmg_precision=0"]
+    r = subprocess.run([MAIN] + args, cwd=tmp_path, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr
+    ours = _iterate_rows(open(tmp_path / "iterate.txt").read())
+    ref = _iterate_rows(g["iterate"])
+    assert len(ours) == len(ref) == 1
+    assert ours[0][0] == ref[0][0] and ours[0][5:] == ref[0][5:], (ours, ref)
+    t_ours, t_ref = _trace(r.stdout), _trace(g["trace"])
+    print("trace ours", t_ours)
+    print("trace ref ", t_ref)
+    assert len(t_ours) == len(t_ref) == 2
+    for k in (0, 1):
+        assert [w for _, w in t_ours[k]] == [w for _, w in t_ref[k]]
+        for (fa, _), (fb, _) in zip(t_ours[k], t_ref[k]):
+            assert abs(fa - fb) <= 2e-5 * abs(fb), (fa, fb)
+    for nm in ("Rv", "Rh"):
+        o = np.fromfile(tmp_path / f"{nm}_iteration_00", np.float32)
+        e = np.asarray(g[f"{nm}_00"], np.float32).ravel()
+        d = np.abs(np.log(o) - np.log(e)).max()
+        step = np.abs(np.log(e) - np.log(rho.ravel())).max()
+        print(f"{tag} {nm}: max |dlog| {d:.2e} (model step {step:.2e})")
+        assert d <= 1e-3 * max(step, 1e-6) + 1e-6, (nm, d, step)
+    if tag == "bound":
+        # below the sea floor plus one cell the model stays inside [0.5, 3]
+        o = np.fromfile(tmp_path / "Rv_iteration_00", np.float32).reshape(rho.shape)
+        zc = start.oz + (np.arange(start.nz) + 0.5) * start.dz
+        below = zc > 1000.0 + start.dz
+        assert o[below].min() >= 0.5 * (1 - 1e-6) and o[below].max() <= 3 * (1 + 1e-6)
