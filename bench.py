@@ -366,6 +366,7 @@ def main():
                    "loss_end": round(float(tr["loss"][-1]), 4)}
 
     solver = make_solver(w, G.PREC_MIXED, a.tol, krylov=a.krylov)
+    shapes, _ = solver.sweep_shapes()
     if W is not None:
         solver.set_learned(W)
     ext = torch.cuda.ExternalStream(solver.stream)
@@ -521,7 +522,10 @@ def main():
                                       " + learned 3x3x3 conv correction after each cycle"),
                        "outer": f"FGMRES({a.krylov})" if a.krylov else "FP64 refinement",
                        "cycle": "F(1,1)", "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (25 x 128^3 systems, ~12 GB)"},
+                       "l2": "inputs larger than L2 (25 x 128^3 systems, ~12 GB)",
+                       "sweep_shapes": {"xyz": [list(v) for v in shapes],
+                                        "fields": "substitution lines/block, ring rows, "
+                                                  "rhs threads/block (set-up autotuner)"}},
             "cycles_mean": float(np.mean(cycles)), "refinements_mean": float(np.mean(refs)),
             "max_rel_residual": float(max(rels)), "all_converged": ok,
             "learned": learned, "mixed_without_learned": without,

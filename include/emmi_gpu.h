@@ -78,6 +78,12 @@ typedef struct {
                        1/d in fp32 (fp32 throughout if an L value leaves
                        the fp16 range), 1 = fp32; 0 = factor in every
                        sweep (2)                                           */
+  int autotune;     /* MIXED with stored fp16 factors: time the level-0
+                       line sweep of each direction at set-up for a few
+                       block shapes and keep the fastest; cached for the
+                       process per (grid, RHS, direction); no shape changes
+                       any result (1); 0 = default shapes; -k (k = 1..10)
+                       forces shape k in every direction (checks)          */
 } emmi_options;
 
 typedef struct {
@@ -120,6 +126,11 @@ size_t emmi_solver_device_bytes(const emmi_solver *s);
 int emmi_solver_line_factor_format(const emmi_solver *s);
 /* The CUDA stream (cudaStream_t) every launch of this solver goes to. */
 void *emmi_solver_stream(const emmi_solver *s);
+/* the level-0 sweep shapes in use per direction d: shapes[d] = {lines per
+ * block and ring depth of the fp16 substitution, threads per block of the
+ * right-hand-side kernel}; *tuned = 1 when this solver's set-up timed them
+ * (0: defaults or the process cache).  No counterpart in the reference. */
+int emmi_solver_sweep_shapes(const emmi_solver *s, int shapes[3][3], int *tuned);
 /* Time `reps` full level-0 line-relaxation sweeps (4 colours, all RHS) along
  * direction dir with CUDA events on the solver's stream, on the solver's
  * current fields.  ms: average milliseconds per sweep; launches: kernel

@@ -1064,16 +1064,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_subst(const int* __restr
 // The same substitution with kFacF16 factors of group grp[rhs] (gstride
 // values per group): the forward pass streams LA, LB and ID, the backward
 // pass LA and LB; the fp16 values are widened to fp32 and the arithmetic is
-// k_line_subst's.
-__global__ void __launch_bounds__(kSolveThreads) k_line_subst_h(const int* __restrict__ active,
-                                                                const int* __restrict__ grp,
-                                                                long nl, int m, long gstride,
-                                                                const float* __restrict__ fac,
-                                                                float2* __restrict__ rb) {
-  __shared__ uint4 ra[kRing][kSolveThreads];
-  __shared__ uint32_t rl5[kRing][kSolveThreads];
-  __shared__ float2 rd[kRing][kSolveThreads];
-  __shared__ float2 rring[kRing][kSolveThreads];
+// k_line_subst's.  NT lines per block, a cp.async ring of RING rows per
+// line: every thread's arithmetic is the same for every (NT, RING).
+template <int NT, int RING>
+__global__ void __launch_bounds__(NT) k_line_subst_h(const int* __restrict__ active,
+                                                     const int* __restrict__ grp, long nl, int m,
+                                                     long gstride, const float* __restrict__ fac,
+                                                     float2* __restrict__ rb) {
+  constexpr int kRing = RING;
+  __shared__ uint4 ra[kRing][NT];
+  __shared__ uint32_t rl5[kRing][NT];
+  __shared__ float2 rd[kRing][NT];
+  __shared__ float2 rring[kRing][NT];
   const int rhs = blockIdx.y;
   if (active && !active[rhs]) return;
   const int tid = threadIdx.x;
@@ -1201,24 +1203,51 @@ static void line_factor_d(const LevelView<T>& L, int color, T* buf, T* fac, int 
   k_line_factor<T, kFacF32><<<g2, kSolveThreads, 0, st>>>(nl, m, gstride, buf, fac, ovf);
 }
 
+// the fp16-factor substitution's block shapes (threads per block, ring
+// depth); variant 0 is the default
+constexpr int kSubstShape[kSubstVariants][2] = {{64, 6}, {32, 6}, {128, 6}, {64, 4}, {64, 8}};
+
+int subst_variant_threads(int v) { return kSubstShape[v][0]; }
+int subst_variant_ring(int v) { return kSubstShape[v][1]; }
+
+template <int NT, int RING>
+static void subst_h_launch(long nl, int nrhs, const int* active, const int* grp, int m,
+                           long gstride, const float* fac, float2* rb, cudaStream_t st) {
+  dim3 g((unsigned)((nl + NT - 1) / NT), nrhs);
+  k_line_subst_h<NT, RING><<<g, NT, 0, st>>>(active, grp, nl, m, gstride, fac, rb);
+}
+
+static void subst_h_variant(int v, long nl, int nrhs, const int* active, const int* grp, int m,
+                            long gstride, const float* fac, float2* rb, cudaStream_t st) {
+  switch (v) {
+    case 1: subst_h_launch<32, 6>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
+    case 2: subst_h_launch<128, 6>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
+    case 3: subst_h_launch<64, 4>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
+    case 4: subst_h_launch<64, 8>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
+    default: subst_h_launch<64, 6>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
+  }
+}
+
 template <typename T, int D>
 static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, const int* grp,
-                             C_t<T>* rb, int fmt, cudaStream_t st) {
+                             C_t<T>* rb, int fmt, SweepShape sh, cudaStream_t st) {
   const int pa = color & 1, pb = (color >> 1) & 1;
   const long nl = line_count(L.n, D, color);
   if (nl == 0) return;
   const long items = nl * L.n[D];
   const int m = 5 * L.n[D] - 4;
   dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
-  dim3 gr((unsigned)(((D == 0 ? 5 : 1) * items + 255) / 256), L.nrhs);
+  const int rt = sh.rhs_threads == 128 ? 128 : 256;
+  dim3 gr((unsigned)(((D == 0 ? 5 : 1) * items + rt - 1) / rt), L.nrhs);
   const LineDiv dv = line_div<D>(L.n, pa, pb);
-  k_line_rhs<T, D><<<gr, 256, 0, st>>>(L, pa, pb, dv, rb);
+  k_line_rhs<T, D><<<gr, rt, 0, st>>>(L, pa, pb, dv, rb);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
   bool done = false;
   if constexpr (std::is_same<T, float>::value) {
     if (fmt == kFacF16) {
-      k_line_subst_h<<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m,
-                                                   line_factor_elems(L.n, D, color, fmt), fac, rb);
+      const int v = sh.subst >= 0 && sh.subst < kSubstVariants ? sh.subst : 0;
+      subst_h_variant(v, nl, L.nrhs, L.active, grp, m, line_factor_elems(L.n, D, color, fmt), fac,
+                      rb, st);
       done = true;
     }
   }
@@ -1256,7 +1285,15 @@ void init_line_kernels() {
                          cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_line_subst<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_subst_h, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(k_line_subst_h<64, 6>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_subst_h<32, 6>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_subst_h<128, 6>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_subst_h<64, 4>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_subst_h<64, 8>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_line_factor<float, kFacF32>,
                          cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -1293,10 +1330,10 @@ void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch
 
 template <typename T>
 void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
-                           C_t<T>* rb, int fmt, cudaStream_t st) {
-  if (d == 0) line_sweep_fac_d<T, 0>(L, color, fac, grp, rb, fmt, st);
-  else if (d == 1) line_sweep_fac_d<T, 1>(L, color, fac, grp, rb, fmt, st);
-  else line_sweep_fac_d<T, 2>(L, color, fac, grp, rb, fmt, st);
+                           C_t<T>* rb, int fmt, cudaStream_t st, SweepShape sh) {
+  if (d == 0) line_sweep_fac_d<T, 0>(L, color, fac, grp, rb, fmt, sh, st);
+  else if (d == 1) line_sweep_fac_d<T, 1>(L, color, fac, grp, rb, fmt, sh, st);
+  else line_sweep_fac_d<T, 2>(L, color, fac, grp, rb, fmt, sh, st);
 }
 
 // ------------------------------------------------------------ point sweep
@@ -1619,7 +1656,7 @@ EMMI_INST(double)
 template void launch_line_factor<float>(const LevelView<float>&, int, int, C_t<float>*, float*,
                                         int, int*, cudaStream_t);
 template void launch_line_sweep_fac<float>(const LevelView<float>&, int, int, const float*,
-                                           const int*, C_t<float>*, int, cudaStream_t);
+                                           const int*, C_t<float>*, int, cudaStream_t, SweepShape);
 template void launch_residual<float, float>(const LevelView<float>&, C_t<float>*, double*, cudaStream_t);
 template void launch_residual<double, double>(const LevelView<double>&, C_t<double>*, double*, cudaStream_t);
 template void launch_residual<double, float>(const LevelView<double>&, C_t<float>*, double*, cudaStream_t);

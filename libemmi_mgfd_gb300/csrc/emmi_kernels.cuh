@@ -45,9 +45,20 @@ long line_factor_elems(const int n[3], int d, int color, int fmt);
 template <typename T>
 void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
                         int fmt, int* ovf, cudaStream_t st);
+// block shapes of a stored-factor sweep: the fp16 substitution's variant
+// (subst_variant_threads lines per block, a cp.async ring of
+// subst_variant_ring rows; 0 = 64 x 6) and the right-hand-side kernel's
+// threads per block (256 or 128).  No shape changes any thread's arithmetic.
+constexpr int kSubstVariants = 5;
+struct SweepShape {
+  int subst = 0;
+  int rhs_threads = 256;
+};
+int subst_variant_threads(int v);
+int subst_variant_ring(int v);
 template <typename T>
 void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
-                           C_t<T>* rb, int fmt, cudaStream_t st);
+                           C_t<T>* rb, int fmt, cudaStream_t st, SweepShape sh = SweepShape());
 
 template <typename T>
 void launch_point_sweep(const LevelView<T>& L, int color, cudaStream_t st);

@@ -22,7 +22,9 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
+#include <map>
 #include <mutex>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -338,7 +340,7 @@ static void line_colour(emmi_solver* s, int h, int l, int d, int col, const Leve
       const long off = s->fac_off[l == 0 ? 0 : h][l][d][col];
       if (off >= 0) {
         launch_line_sweep_fac<float>(W, d, col, s->d_fac + off, s->d_grp + r0,
-                                     (C_t<float>*)s->scratch, s->fac_fmt, s->st);
+                                     (C_t<float>*)s->scratch, s->fac_fmt, s->st, s->shape[l][d]);
         return;
       }
     }
@@ -590,6 +592,101 @@ static int build_line_factors(emmi_solver* s) {
   return EMMI_OK;
 }
 
+// ---- autotuning of the level-0 sweep shapes ------------------------------
+// The stored-factor line sweep of each direction is timed at set-up on this
+// solver's own level-0 operators (zero fields) for a few block shapes -- the
+// right-hand-side kernel's threads per block, then the fp16 substitution's
+// lines per block and ring depth -- and the fastest is kept when it beats
+// the incumbent by more than 2 %.  No shape changes any result.  Choices are
+// cached for the process by (grid, RHS per launch, RHS, factor format,
+// direction), so later solvers of the same shape take them without timing.
+static std::mutex g_tune_mu;
+static std::map<std::array<long, 7>, emmi::SweepShape> g_tune;
+
+static int autotune_sweeps(emmi_solver* s) {
+  if (!s->fac_on || s->fac_fmt != kFacF16 || !s->opt.isemicoarsen || s->lmax < 2) return EMMI_OK;
+  bool ready = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  for (int d = 0; d < 3; d++) {
+    int h = -1;
+    for (int c = 0; c < 3 && h < 0; c++)
+      if (s->hier[c][1].sc[d] == 2) h = c;
+    if (h < 0) continue;
+    const HLev& L0 = s->hier[h][0];
+    const std::array<long, 7> key = {L0.n[0], L0.n[1], L0.n[2], s->chunk, s->nrhs, s->fac_fmt, d};
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        s->shape[0][d] = it->second;
+        continue;
+      }
+    }
+    if (!ready) {
+      std::vector<int> all(s->nrhs, 1);
+      CK(cudaMemcpyAsync(s->d_active, all.data(), s->nrhs * sizeof(int), cudaMemcpyHostToDevice,
+                         s->st));
+      const size_t fb = (size_t)3 * s->hier[0][0].S * s->nrhs * sizeof(float2);
+      CK(cudaMemsetAsync(s->u32[0], 0, fb, s->st));
+      CK(cudaMemsetAsync(s->f32[0], 0, fb, s->st));
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      ready = true;
+    }
+    auto sweep = [&]() {
+      for (int cc = 0; cc < 4; cc++)
+        for (int r0 = 0; r0 < s->nrhs; r0 += s->chunk) {
+          LevelView<float> W = s->view<float>(h, 0);
+          W.nrhs = std::min(s->chunk, s->nrhs - r0);
+          W.u += (long)r0 * 3 * W.S;
+          W.f += (long)r0 * 3 * W.S;
+          W.r += (long)r0 * 3 * W.S;
+          W.wmu += r0;
+          W.active += r0;
+          W.op += r0;
+          line_colour<float>(s, h, 0, d, cc, W, r0);
+        }
+    };
+    auto time_shape = [&](SweepShape sh) -> float {
+      s->shape[0][d] = sh;
+      sweep();
+      cudaEventRecord(e0, s->st);
+      sweep();
+      sweep();
+      cudaEventRecord(e1, s->st);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        return 1e30f;
+      return ms;
+    };
+    SweepShape best;
+    float best_ms = time_shape(best);
+    auto consider = [&](SweepShape c) {
+      const float t = time_shape(c);
+      if (t < 0.98f * best_ms) {
+        best = c;
+        best_ms = t;
+      }
+    };
+    SweepShape c = best;
+    c.rhs_threads = 128;
+    consider(c);
+    for (int v = 1; v < kSubstVariants; v++) {
+      c = best;
+      c.subst = v;
+      consider(c);
+    }
+    s->shape[0][d] = best;
+    s->tuned_now = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = best;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  return EMMI_OK;
+}
+
 // Stored FP64 coefficients of the level-0 true operators for the mixed
 // solver's refinement residual, when they fit in half of the free device
 // memory (else the residual computes them, as the FP64 solver does)
@@ -637,6 +734,7 @@ void emmi_default_options(emmi_options* o) {
   o->verb = 0;
   o->krylov = 0;
   o->line_factors = 2;
+  o->autotune = 1;
 }
 
 static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
@@ -959,6 +1057,17 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
     mark("field buffers");
     if (mixed && s->opt.line_factors) TRY(build_line_factors(s));
     mark("line factors");
+    if (mixed && s->opt.autotune > 0) TRY(autotune_sweeps(s));
+    if (mixed && s->opt.autotune < 0) {
+      // a forced level-0 shape k = -autotune (1..10): substitution variant
+      // (k-1) % 5, right-hand-side threads 256 for k <= 5, else 128
+      const int k = std::min(-s->opt.autotune, 2 * kSubstVariants) - 1;
+      for (int d = 0; d < 3; d++) {
+        s->shape[0][d].subst = k % kSubstVariants;
+        s->shape[0][d].rhs_threads = k < kSubstVariants ? 256 : 128;
+      }
+    }
+    mark("sweep shapes");
     if (mixed) TRY(build_coef64(s));
     mark("FP64 coefficients");
   }
@@ -1291,6 +1400,21 @@ int emmi_solver_solve_resident(emmi_solver* s, double* x_dev, double* h_dev,
 }
 
 void* emmi_solver_stream(const emmi_solver* s) { return s ? (void*)s->st : nullptr; }
+
+int emmi_solver_sweep_shapes(const emmi_solver* s, int shapes[3][3], int* tuned) {
+  if (!s || !shapes) {
+    set_err("emmi_solver_sweep_shapes: bad argument");
+    return EMMI_EINVAL;
+  }
+  for (int d = 0; d < 3; d++) {
+    const SweepShape& sh = s->shape[0][d];
+    shapes[d][0] = subst_variant_threads(sh.subst);
+    shapes[d][1] = subst_variant_ring(sh.subst);
+    shapes[d][2] = sh.rhs_threads;
+  }
+  if (tuned) *tuned = s->tuned_now ? 1 : 0;
+  return EMMI_OK;
+}
 
 int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int* launches,
                               double* bytes) {

@@ -29,6 +29,11 @@ struct emmi_solver {
   int gmax1, gstride;
   emmi::HLev hier[3][emmi::kMaxLev];
   bool has_norm;  // the cycle has a level-0 norm test
+  // block shapes of the stored-factor sweeps per (level, direction): the
+  // level-0 ones picked at set-up by timing (opt.autotune), the rest the
+  // defaults
+  emmi::SweepShape shape[emmi::kMaxLev][3];
+  bool tuned_now = false;  // set-up timed shapes (not taken from the cache)
 
   // device memory
   std::vector<void*> allocs;

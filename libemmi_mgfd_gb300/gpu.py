@@ -51,7 +51,7 @@ class _Options(C.Structure):
                 ("tol", C.c_double), ("isemicoarsen", C.c_int), ("precision", C.c_int),
                 ("sigma_floor", C.c_double), ("refine_every", C.c_int),
                 ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int),
-                ("line_factors", C.c_int)]
+                ("line_factors", C.c_int), ("autotune", C.c_int)]
 
 
 class _Stats(C.Structure):
@@ -106,11 +106,12 @@ class Options:
     verb: int = 0
     krylov: int = 0
     line_factors: int = 2
+    autotune: int = 1
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
                         self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
-                        self.verb, self.krylov, self.line_factors)
+                        self.verb, self.krylov, self.line_factors, self.autotune)
 
 
 class Solver:
@@ -313,6 +314,15 @@ class Solver:
     @property
     def device_bytes(self) -> int:
         return lib().emmi_solver_device_bytes(self._h)
+
+    def sweep_shapes(self):
+        """([(lines per block, ring depth, rhs threads)] per direction of the
+        level-0 sweeps, tuned at this solver's set-up)."""
+        sh = ((C.c_int * 3) * 3)()
+        tuned = C.c_int()
+        _check(lib().emmi_solver_sweep_shapes(self._h, sh, C.byref(tuned)),
+               "emmi_solver_sweep_shapes")
+        return [tuple(sh[d]) for d in range(3)], bool(tuned.value)
 
     @property
     def line_factor_format(self) -> int:

@@ -288,3 +288,40 @@ def test_pooled_memory_is_reused_and_trimmed(golden):
         s.close()
     assert G.lib().emmi_trim_memory() == 0
     torch.cuda.synchronize()
+
+
+@gpu
+def test_sweep_shapes_never_change_the_result(golden):
+    """Every level-0 sweep shape the autotuner chooses from (forced one at a
+    time) gives the defaults' iterates bit for bit; the autotuner times the
+    shapes on a new grid and a second solver of the same shape takes them
+    from the process cache."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"]])
+    oms = np.array([om, om, 0.5 * om], np.float32)
+
+    def run(autotune):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
+                     op=np.zeros(3, np.int32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=6, tol=0.0,
+                                       sigma_floor=2e-4, autotune=autotune))
+        x, h, st = s.solve(bs)
+        shapes = s.sweep_shapes()
+        s.close()
+        return x, h, shapes
+
+    x0, h0, (sh0, _) = run(0)
+    assert all(sh == (64, 6, 256) for sh in sh0), sh0
+    seen = set()
+    for k in range(1, 11):
+        x, h, (sh, tuned) = run(-k)
+        assert not tuned
+        seen.add(sh[0])
+        assert np.array_equal(x, x0) and np.array_equal(h, h0), (k, sh)
+    assert len(seen) == 10
+    _, _, (sh1, tuned1) = run(1)
+    x2, h2, (sh2, tuned2) = run(1)
+    assert sh1 == sh2 and not tuned2
+    assert np.array_equal(x2, x0)
