@@ -25,7 +25,9 @@
 #include <map>
 #include <mutex>
 #include <array>
+#include <cctype>
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -602,6 +604,71 @@ static int build_line_factors(emmi_solver* s) {
 // direction), so later solvers of the same shape take them without timing.
 static std::mutex g_tune_mu;
 static std::map<std::array<long, 7>, emmi::SweepShape> g_tune;
+static bool g_tune_loaded = false;
+
+// The cache persists across processes in the JSON file named by
+// EMMI_TUNE_FILE when that is set: read once before the first tuning,
+// rewritten whole after every new entry.  Each entry lists, in this order,
+// grid (3), chunk, nrhs, fmt, dir, subst, rhs_threads; entries that do not
+// read as nine integers are skipped.  Call with g_tune_mu held.
+static void tune_file_load() {
+  g_tune_loaded = true;
+  const char* path = std::getenv("EMMI_TUNE_FILE");
+  if (!path || !*path) return;
+  FILE* fp = std::fopen(path, "r");
+  if (!fp) return;
+  std::string text;
+  char buf[4096];
+  size_t k;
+  while ((k = std::fread(buf, 1, sizeof(buf), fp)) > 0) text.append(buf, k);
+  std::fclose(fp);
+  size_t pos = text.find("\"sweep_shapes\"");
+  while (pos != std::string::npos) {
+    const size_t a = text.find('{', pos + 1), b = a == std::string::npos ? a : text.find('}', a);
+    if (a == std::string::npos || b == std::string::npos) break;
+    long v[9];
+    int nv = 0;
+    for (size_t i = a; i < b && nv < 9;) {
+      if (std::isdigit((unsigned char)text[i])) {
+        size_t e = i;
+        while (e < b && std::isdigit((unsigned char)text[e])) e++;
+        v[nv++] = std::strtol(text.substr(i, e - i).c_str(), nullptr, 10);
+        i = e;
+      } else {
+        i++;
+      }
+    }
+    if (nv == 9 && v[7] >= 0 && v[7] < kSubstVariants && (v[8] == 128 || v[8] == 256)) {
+      emmi::SweepShape sh;
+      sh.subst = (int)v[7];
+      sh.rhs_threads = (int)v[8];
+      g_tune[{v[0], v[1], v[2], v[3], v[4], v[5], v[6]}] = sh;
+    }
+    pos = b;
+  }
+}
+
+static void tune_file_save() {
+  const char* path = std::getenv("EMMI_TUNE_FILE");
+  if (!path || !*path) return;
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* fp = std::fopen(tmp.c_str(), "w");
+  if (!fp) return;
+  std::fprintf(fp, "{\"sweep_shapes\": [");
+  bool first = true;
+  for (const auto& kv : g_tune) {
+    const auto& q = kv.first;
+    std::fprintf(fp,
+                 "%s\n  {\"grid\": [%ld, %ld, %ld], \"chunk\": %ld, \"nrhs\": %ld, \"fmt\": %ld, "
+                 "\"dir\": %ld, \"subst\": %d, \"rhs_threads\": %d}",
+                 first ? "" : ",", q[0], q[1], q[2], q[3], q[4], q[5], q[6], kv.second.subst,
+                 kv.second.rhs_threads);
+    first = false;
+  }
+  std::fprintf(fp, "\n]}\n");
+  std::fclose(fp);
+  std::rename(tmp.c_str(), path);
+}
 
 static int autotune_sweeps(emmi_solver* s) {
   if (!s->fac_on || s->fac_fmt != kFacF16 || !s->opt.isemicoarsen || s->lmax < 2) return EMMI_OK;
@@ -616,6 +683,7 @@ static int autotune_sweeps(emmi_solver* s) {
     const std::array<long, 7> key = {L0.n[0], L0.n[1], L0.n[2], s->chunk, s->nrhs, s->fac_fmt, d};
     {
       std::lock_guard<std::mutex> lk(g_tune_mu);
+      if (!g_tune_loaded) tune_file_load();
       auto it = g_tune.find(key);
       if (it != g_tune.end()) {
         s->shape[0][d] = it->second;
@@ -680,6 +748,7 @@ static int autotune_sweeps(emmi_solver* s) {
     s->tuned_now = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = best;
+    tune_file_save();
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

@@ -325,3 +325,47 @@ def test_sweep_shapes_never_change_the_result(golden):
     x2, h2, (sh2, tuned2) = run(1)
     assert sh1 == sh2 and not tuned2
     assert np.array_equal(x2, x0)
+
+
+_TUNE_CHILD = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from libemmi_mgfd_gb300 import gpu as G
+n = (12, 12, 12)
+rng = np.random.default_rng(5)
+raw = np.concatenate([10.0 ** rng.uniform(-2, 0, (3,) + n[::-1]),
+                      np.ones((1,) + n[::-1])]).astype(np.float32)
+x = [np.arange(v + 1, dtype=np.float32) * 100.0 for v in n]
+s = G.Solver(n, *x, raw[None], np.full(2, 6.28, np.float32), op=np.zeros(2, np.int32),
+             options=G.Options(precision=G.PREC_MIXED, ncycle=2, tol=0.0))
+print(json.dumps(s.sweep_shapes()))
+s.close()
+"""
+
+
+@gpu
+def test_tuned_shapes_persist_as_json(tmp_path):
+    """With EMMI_TUNE_FILE the autotuner's choices outlive the process: a
+    first process times the shapes and writes them as JSON, a second one
+    reads them back and times nothing."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = tmp_path / "tune.json"
+    env = dict(os.environ, EMMI_TUNE_FILE=str(path))
+    out = []
+    for _ in range(2):
+        r = subprocess.run([sys.executable, "-c", _TUNE_CHILD, root], env=env,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    (sh1, tuned1), (sh2, tuned2) = out
+    assert tuned1 and not tuned2 and sh1 == sh2
+    doc = json.loads(path.read_text())
+    entries = doc["sweep_shapes"]
+    assert len(entries) >= 1
+    for e in entries:
+        assert e["grid"] == [12, 12, 12] and e["nrhs"] == 2 and e["rhs_threads"] in (128, 256)
