@@ -369,3 +369,52 @@ def test_tuned_shapes_persist_as_json(tmp_path):
     assert len(entries) >= 1
     for e in entries:
         assert e["grid"] == [12, 12, 12] and e["nrhs"] == 2 and e["rhs_threads"] in (128, 256)
+
+
+@gpu
+def test_config2_batch_mixed_matches_fp64_solve():
+    """The batched configuration at full size -- 25 shots x 2 frequencies
+    (0.25, 0.75 Hz) = 50 right-hand sides on 25 operators in one solver,
+    96^3 mesh, VTI sediment, random bathymetry, a resistive box, 200
+    receivers: every mixed-precision solve converges to 1e-8 and its
+    receiver data agree with an FP64 solve of the same batch to 1e-10
+    within 1e-4 of each channel's largest value (channels above 1e-3 of
+    the batch's largest)."""
+    from libemmi_mgfd_gb300 import host
+    from libemmi_mgfd_gb300 import workloads as W
+    G = _G()
+    s = W.config2(96)
+    m = host.Model.from_survey(s)
+    src = s.sources.astype(np.float32).copy()
+    src[:, 3:] = np.deg2rad(src[:, 3:])
+    rec = s.receivers.astype(np.float32).copy()
+    rec[:, 3:] = np.deg2rad(rec[:, 3:])
+    grids = [m.regrid(float(p[0]), float(p[1]), float(p[2])) for p in s.sources]
+    X = [np.stack([g[k] for g in grids]) for k in ("x1", "x2", "x3")]
+    cells = np.stack([np.stack([g["sigma11"], g["sigma22"], g["sigma33"], g["invmur"]])
+                      for g in grids])
+    nf = len(s.freqs)
+    om = np.array([2 * np.pi * s.freqs[r % nf] for r in range(len(src) * nf)], np.float32)
+    op = np.repeat(np.arange(len(src), dtype=np.int32), nf)
+    srcr = np.repeat(src, nf, axis=0)
+    out = {}
+    for prec, tol in ((G.PREC_MIXED, 1e-8), (G.PREC_FP64, 1e-10)):
+        sv = G.Solver(s.n, *X, cells, om, op=op,
+                      options=G.Options(precision=prec, tol=tol, ncycle=100),
+                      rho_water=np.float32(m.rho_water()))
+        d, st, _ = sv.modelling(srcr, rec, s.chsrc, s.chrec)
+        sv.close()
+        assert all(q["status"] == "ok" for q in st), [q["status"] for q in st]
+        out[prec] = (d, np.mean([q["cycles"] for q in st]))
+    d, d64 = out[G.PREC_MIXED][0], out[G.PREC_FP64][0]
+    print("cycles mixed / fp64:", out[G.PREC_MIXED][1], out[G.PREC_FP64][1])
+    top = np.abs(d64).max()
+    worst = 0.0
+    for r in range(d.shape[0]):
+        for c in range(d.shape[1]):
+            mx = np.abs(d64[r, c]).max()
+            if mx < 1e-3 * top:
+                continue
+            worst = max(worst, float(np.abs(d[r, c] - d64[r, c]).max() / mx))
+    print(f"largest receiver error vs FP64: {worst:.2e}")
+    assert worst < 1e-4, worst
