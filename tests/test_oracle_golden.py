@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's own outputs (tests/golden/, made by
 the reference compiled from its sources).  This pins the oracle before it
-judges the CUDA path.
+checks the CUDA path.
 
 Below the sea surface and in H the oracle reproduces the reference to
 roundoff; in the air layer (sigma = 1e-8 S/m) the curl-free part of E is
