@@ -303,9 +303,19 @@ typedef struct {
 void emmi_dropin_options(emmi_options *o, int verb);
 
 typedef struct emmi_fg emmi_fg;
-/* copies the survey, data and masks to the device once per inversion */
+/* copies the survey, data and masks to the device once per inversion; with
+ * dobs and delta NULL only emmi_fg_forward may run (npar, idxpar, bathy
+ * and the mutes are then not read) */
 int emmi_fg_create(emmi_fg **out, const emmi_fg_problem *P,
                    const emmi_options *opts);
+/* Forward modelling of every shot and frequency in one solver
+ * (do_modelling, src/do_modelling.c:49-67, for all shots at once): the
+ * homogenization of the padded model, injection, solve, receiver data
+ * dcal [nshot][nrec_ch][nfreq][nrec] (complex, interleaved); stats (may be
+ * NULL) [nshot*nfreq].  Host arrays; synchronises. */
+int emmi_fg_forward(emmi_fg *f, int nxp, int nyp, int nzp, const float *xx,
+                    const float *yy, const float *zz, const float *pad,
+                    float *dcal, emmi_rhs_stats *stats);
 /* One evaluation at the model whose padded form is xx, yy, zz, pad
  * (eh_pad_model) and whose input-grid resistivities are rho11, rho33
  * [nz][ny][nx]: fcost [nshot] each shot's 0.5*|W(dobs - dcal)|^2, grad and

@@ -334,9 +334,10 @@ static float gradient_shot(fg_ctx *c, shot_t *t) {
 }
 
 /* the batched evaluation (batch=1): every shot's mesh axes (the padded
- * model's node axes do not depend on the resistivities), the survey, the
- * observed data and the uncertainties go to the device once */
-static void fg_batch_init(fg_ctx *c) {
+ * model's node axes do not depend on the resistivities), the survey and,
+ * with_data, the observed data and the uncertainties go to the device once;
+ * without them only the forward modelling of mode=0 runs */
+static void fg_batch_init(fg_ctx *c, int with_data) {
   emmi_emf_t *emf = c->emf;
   emmi_fwi_t *fwi = c->fwi;
   const int ns = c->nshots, nf = emf->nfreq, nch = emf->nchrec;
@@ -388,17 +389,20 @@ static void fg_batch_init(fg_ctx *c) {
       p[3] = t->raz[ir];
       p[4] = t->rdip[ir];
     }
-    for (int ic = 0; ic < nch; ic++)
-      for (int f = 0; f < nf; f++)
-        for (int ir = 0; ir < t->nrec; ir++) {
-          const size_t from = ((size_t)ic * nf + f) * t->nrec + ir;
-          const size_t to = (((size_t)is * nch + ic) * nf + f) * maxrec + ir;
-          dobs[to] = t->dobs[from];
-          delta[to] = t->delta[from];
-        }
+    if (with_data)
+      for (int ic = 0; ic < nch; ic++)
+        for (int f = 0; f < nf; f++)
+          for (int ir = 0; ir < t->nrec; ir++) {
+            const size_t from = ((size_t)ic * nf + f) * t->nrec + ir;
+            const size_t to = (((size_t)is * nch + ic) * nf + f) * maxrec + ir;
+            dobs[to] = t->dobs[from];
+            delta[to] = t->delta[from];
+          }
   }
   int *src_ch = malloc(emf->nchsrc * sizeof(int));
   for (int k = 0; k < emf->nchsrc; k++) src_ch[k] = chan_code(emf->chsrc[k]);
+  int *rec_ch = malloc(nch * sizeof(int));
+  for (int k = 0; k < nch; k++) rec_ch[k] = chan_code(emf->chrec[k]);
   emmi_fg_problem P;
   memset(&P, 0, sizeof(P));
   P.nx = emf->nx;
@@ -423,19 +427,21 @@ static void fg_batch_init(fg_ctx *c) {
   P.nsrc_ch = emf->nchsrc;
   P.src_ch = src_ch;
   P.nrec_ch = nch;
-  P.rec_ch = c->chc;
+  P.rec_ch = rec_ch;
   P.nrec = maxrec;
   P.nrec_shot = nrs;
   P.src = src;
   P.rec = rec;
-  P.dobs = (const float *)dobs;
-  P.delta = delta;
-  P.npar = fwi->npar;
-  P.idxpar = fwi->idxpar;
-  P.preco = fwi->preco;
-  P.bathy = &emf->bathy[0][0];
-  P.dsmute = emf->dsmute;
-  P.drmute = emf->drmute;
+  if (with_data) {
+    P.dobs = (const float *)dobs;
+    P.delta = delta;
+    P.npar = fwi->npar;
+    P.idxpar = fwi->idxpar;
+    P.preco = fwi->preco;
+    P.bathy = &emf->bathy[0][0];
+    P.dsmute = emf->dsmute;
+    P.drmute = emf->drmute;
+  }
   emmi_options opt;
   emmi_dropin_options(&opt, 0);
   if (emmi_fg_create(&c->fg, &P, &opt) != EMMI_OK) die("emmi_fg_create failed: ", emmi_last_error());
@@ -451,6 +457,7 @@ static void fg_batch_init(fg_ctx *c) {
   free(dobs);
   free(delta);
   free(src_ch);
+  free(rec_ch);
 }
 
 /* the data part of fg_fwi for every shot in one device evaluation: the
@@ -953,6 +960,42 @@ int main(int argc, char **argv) {
     if (sh[is].nrec > maxrec) maxrec = sh[is].nrec;
   c.dc = calloc((size_t)emf.nchrec * emf.nfreq * maxrec, sizeof(emmi_cf32));
 
+  /* batch=1 (default): all shots and frequencies in one device solver;
+   * batch=0: shot by shot through the drop-in entry points */
+  int batch = 1;
+  getparint("batch", &batch);
+  if (emf.mode == 0 && batch) {
+    /* ---- do_modelling (src/do_modelling.c:49-67) for every shot at once ---- */
+    fg_batch_init(&c, 0);
+    const int nf = emf.nfreq, nch = emf.nchrec;
+    const size_t nper = (size_t)nshots * nch * nf * c.maxrec;
+    emmi_cf32 *dall = malloc(nper * sizeof(emmi_cf32));
+    emmi_rhs_stats *st = malloc((size_t)nshots * nf * sizeof(emmi_rhs_stats));
+    if (emmi_fg_forward(c.fg, c.nxp, c.nyp, c.nzp, c.pxx, c.pyy, c.pzz, c.pad, (float *)dall,
+                        st) != EMMI_OK)
+      die("emmi_fg_forward failed: ", emmi_last_error());
+    for (int is = 0; is < nshots; is++) {
+      shot_t *t = &sh[is];
+      for (int ic = 0; ic < nch; ic++)
+        for (int f = 0; f < nf; f++) {
+          if (emf.verb && ic == 0) {
+            const emmi_rhs_stats *q = &st[(size_t)is * nf + f];
+            printf("shot %d freq %g: %d cycles, relative residual %.3e, status %d\n", t->shot,
+                   emf.freqs[f], q->cycles, q->rnorm0 > 0 ? q->rnorm / q->rnorm0 : 0., q->status);
+          }
+          for (int ir = 0; ir < t->nrec; ir++)
+            c.dc[((size_t)ic * nf + f) * t->nrec + ir] =
+                dall[(((size_t)is * nch + ic) * nf + f) * c.maxrec + ir];
+        }
+      char fname[64];
+      snprintf(fname, sizeof(fname), "emf_%04d.txt", t->shot);
+      write_data(fname, t->shot, &emf, t->nrec, c.dc);
+    }
+    free(dall);
+    free(st);
+    emmi_fg_destroy(c.fg);
+    return 0;
+  }
   if (emf.mode == 0) {
     /* ---- do_modelling frequency loop (src/do_modelling.c:49-67) ---- */
     for (int is = 0; is < nshots; is++) {
@@ -1034,11 +1077,7 @@ int main(int argc, char **argv) {
     write_data(fname, t->shot, &emf, t->nrec, t->dobs);
     c.ndata += emf.nchrec * emf.nfreq * t->nrec;
   }
-  /* batch=1 (default): all shots and frequencies of an evaluation in one
-   * device solver; batch=0: shot by shot through the drop-in entry points */
-  int batch = 1;
-  getparint("batch", &batch);
-  if (batch) fg_batch_init(&c);
+  if (batch) fg_batch_init(&c, 1);
   if (emf.mode == 2) {
     /* one misfit and gradient at the input model (x = log rho, do_fwi.c:113-124) */
     float *xx = malloc((size_t)fwi.n * sizeof(float)), *g = malloc((size_t)fwi.n * sizeof(float));

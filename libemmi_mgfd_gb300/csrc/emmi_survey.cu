@@ -807,6 +807,7 @@ static void per_rhs_points(int nshot, int nfreq, int nrec, const int* nrec_shot,
 
 struct emmi_fg {
   int nx, ny, nz, n1, n2, n3, nshot, nfreq, nrhs, nrec, nch, nsrc_ch, npar, preco;
+  bool have_data = true;  // observed data and uncertainties given (else forward only)
   float o[3], d[3], rho_water;
   long nxyz, nc;
   std::vector<float> x1, x2, x3, omega_rhs, rho_water_op;
@@ -852,13 +853,17 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
     return EMMI_EINVAL;
   }
   *out = nullptr;
+  // without observed data (dobs and delta NULL) only emmi_fg_forward runs,
+  // and the gradient's parameters and masks are not needed
+  const bool data = P->dobs || P->delta;
   bool ok = P->nx > 0 && P->ny > 0 && P->nz > 0 && P->n1 > 0 && P->n2 > 0 && P->n3 > 0 &&
             P->nshot > 0 && P->nfreq > 0 && (long)P->nshot * P->nfreq <= 65535 && P->omega &&
             P->x1 && P->x2 && P->x3 && P->nsrc_ch >= 1 && P->nsrc_ch <= 6 && P->src_ch &&
             P->nrec_ch >= 1 && P->nrec_ch <= 6 && P->rec_ch && P->nrec >= 1 && P->nrec_shot &&
-            P->src && P->rec && P->dobs && P->delta && P->npar >= 1 && P->npar <= 2 &&
-            P->idxpar && P->bathy && P->rho_water > 0;
-  for (int k = 0; ok && k < P->npar; k++) ok = P->idxpar[k] == 1 || P->idxpar[k] == 2;
+            P->src && P->rec && P->rho_water > 0 &&
+            (!data || (P->dobs && P->delta && P->npar >= 1 && P->npar <= 2 && P->idxpar &&
+                       P->bathy));
+  for (int k = 0; ok && data && k < P->npar; k++) ok = P->idxpar[k] == 1 || P->idxpar[k] == 2;
   for (int k = 0; ok && k < P->nsrc_ch; k++) ok = P->src_ch[k] >= 0 && P->src_ch[k] <= 5;
   for (int k = 0; ok && k < P->nrec_ch; k++) ok = P->rec_ch[k] >= 0 && P->rec_ch[k] <= 5;
   for (int k = 0; ok && k < P->nshot; k++) ok = P->nrec_shot[k] >= 0 && P->nrec_shot[k] <= P->nrec;
@@ -879,8 +884,9 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
   f->nrec = P->nrec;
   f->nch = P->nrec_ch;
   f->nsrc_ch = P->nsrc_ch;
-  f->npar = P->npar;
-  f->preco = P->preco;
+  f->have_data = data;
+  f->npar = data ? P->npar : 1;
+  f->preco = data ? P->preco : 0;
   f->rho_water = P->rho_water;
   for (int e = 0; e < 3; e++) {
     f->o[e] = P->o[e];
@@ -894,7 +900,8 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
   f->rho_water_op.assign(P->nshot, P->rho_water);
   f->src_ch.assign(P->src_ch, P->src_ch + P->nsrc_ch);
   f->rec_ch.assign(P->rec_ch, P->rec_ch + P->nrec_ch);
-  f->idxpar.assign(P->idxpar, P->idxpar + P->npar);
+  if (data) f->idxpar.assign(P->idxpar, P->idxpar + P->npar);
+  else f->idxpar.assign(1, 1);
   for (int r = 0; r < f->nrhs; r++) {
     f->op.push_back(r / P->nfreq);
     f->omega_rhs.push_back(P->omega[r % P->nfreq]);
@@ -903,12 +910,13 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
   std::vector<float> skin(P->nfreq), rsrc, rrec;
   for (int k = 0; k < P->nfreq; k++) skin[k] = misfit_skin(P->omega[k], P->rho_water);
   per_rhs_points(P->nshot, P->nfreq, P->nrec, P->nrec_shot, P->src, P->rec, rsrc, rrec);
-  std::vector<unsigned char> bm, mm;
-  gradient_masks(P->nx, P->ny, P->nz, P->o, P->d, P->bathy, P->nshot, P->src, P->dsmute,
-                 P->nrec, P->nrec_shot, P->rec, P->drmute, 5, bm, mm);
+  std::vector<unsigned char> bm(1, 0), mm(1, 0);
+  if (data)
+    gradient_masks(P->nx, P->ny, P->nz, P->o, P->d, P->bathy, P->nshot, P->src, P->dsmute,
+                   P->nrec, P->nrec_shot, P->rec, P->drmute, 5, bm, mm);
   const size_t nper = (size_t)P->nshot * f->nch * P->nfreq * P->nrec;
   const size_t nrd = (size_t)f->nrhs * f->nch * P->nrec;
-  const size_t ne = (size_t)3 * f->nrhs * f->nxyz;
+  const size_t ne = data ? (size_t)3 * f->nrhs * f->nxyz : 1;  // volume fields: gradient only
   if (cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking) != cudaSuccess ||
       !f->alloc(&f->d_src, rsrc.size()) || !f->alloc(&f->d_rec, rrec.size()) ||
       !f->alloc(&f->d_delta, nper) || !f->alloc(&f->d_skin, P->nfreq) ||
@@ -920,7 +928,7 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
       !f->alloc(&f->d_dcal, nrd) || !f->alloc(&f->d_dres, nrd) || !f->alloc(&f->d_dsyn, nper) ||
       !f->alloc(&f->d_Ef, ne) || !f->alloc(&f->d_Ea, ne) || !f->alloc(&f->d_bm, bm.size()) ||
       !f->alloc(&f->d_mm, mm.size()) || !f->alloc(&f->d_nrec, P->nshot) ||
-      !f->alloc(&f->d_idx, P->npar)) {
+      !f->alloc(&f->d_idx, f->npar)) {
     set_err("emmi_fg_create: device allocation failed");
     emmi_fg_destroy(f);
     return EMMI_ENOMEM;
@@ -928,13 +936,15 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
   cudaStream_t st = f->st;
   cudaMemcpyAsync(f->d_src, rsrc.data(), rsrc.size() * sizeof(float), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(f->d_rec, rrec.data(), rrec.size() * sizeof(float), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(f->d_delta, P->delta, nper * sizeof(float), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(f->d_dobs, P->dobs, nper * sizeof(float2), cudaMemcpyHostToDevice, st);
+  if (data) {
+    cudaMemcpyAsync(f->d_delta, P->delta, nper * sizeof(float), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(f->d_dobs, P->dobs, nper * sizeof(float2), cudaMemcpyHostToDevice, st);
+  }
   cudaMemcpyAsync(f->d_skin, skin.data(), skin.size() * sizeof(float), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(f->d_bm, bm.data(), bm.size(), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(f->d_mm, mm.data(), mm.size(), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(f->d_nrec, P->nrec_shot, P->nshot * sizeof(int), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(f->d_idx, P->idxpar, P->npar * sizeof(int), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(f->d_idx, f->idxpar.data(), f->npar * sizeof(int), cudaMemcpyHostToDevice, st);
   const cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     set_err("emmi_fg_create: %s", cudaGetErrorString(e));
@@ -952,6 +962,10 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
   if (!f || !xx || !yy || !zz || !pad || !rho11 || !rho33 || !fcost || !grad) {
     set_err("emmi_fg_eval: bad argument");
     return EMMI_EINVAL;
+  }
+  if (!f->have_data) {
+    set_err("emmi_fg_eval: created without observed data (forward modelling only)");
+    return EMMI_ESTATE;
   }
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
@@ -1052,6 +1066,57 @@ int emmi_fg_eval(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const f
     }
   }
   for (auto& e : ev) cudaEventDestroy(e);
+  emmi_solver_destroy(s);
+  return rc;
+}
+
+int emmi_fg_forward(emmi_fg* f, int nxp, int nyp, int nzp, const float* xx, const float* yy,
+                    const float* zz, const float* pad, float* dcal, emmi_rhs_stats* stats) {
+  if (!f || !xx || !yy || !zz || !pad || !dcal) {
+    set_err("emmi_fg_forward: bad argument");
+    return EMMI_EINVAL;
+  }
+  int rc = emmi_homogenize_batch(nxp, nyp, nzp, xx, yy, zz, pad, f->nshot, f->n1, f->n2, f->n3,
+                                 f->x1.data(), f->x2.data(), f->x3.data(), f->d_cells, f->st);
+  if (rc != EMMI_OK) return rc;
+  emmi_problem P = {f->n1,         f->n2,        f->n3,        f->nshot,
+                    f->nrhs,       f->x1.data(), f->x2.data(), f->x3.data(),
+                    f->d_cells,    f->op.data(), f->omega_rhs.data(), f->rho_water_op.data()};
+  emmi_solver* s = nullptr;
+  if ((rc = emmi_solver_create_dc(&s, &P, &f->opt)) != EMMI_OK) return rc;
+  double* E = (double*)s->u64[0];
+  double* H = (double*)s->f64[0];
+  std::vector<emmi_rhs_stats> tmp;
+  if (!stats) {
+    tmp.resize(f->nrhs);
+    stats = tmp.data();
+  }
+  rc = emmi_inject_sources_dev(s, f->d_src, f->nsrc_ch, f->src_ch.data(), E);
+  if (rc == EMMI_OK) rc = emmi_solver_solve_resident(s, nullptr, nullptr, stats);
+  if (rc == EMMI_OK)
+    rc = emmi_extract_receivers_dev(s, f->d_rec, f->nrec, f->nch, f->rec_ch.data(), E, H,
+                                    (float*)f->d_dcal);
+  if (rc == EMMI_OK) {
+    // [shot * nfreq + f][c][ir] on the device -> [shot][c][f][ir]
+    const size_t nrd = (size_t)f->nrhs * f->nch * f->nrec;
+    std::vector<float2> h(nrd);
+    cudaMemcpyAsync(h.data(), f->d_dcal, nrd * sizeof(float2), cudaMemcpyDeviceToHost, s->st);
+    const cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+      set_err("emmi_fg_forward: %s", cudaGetErrorString(e));
+      rc = EMMI_ECUDA;
+    } else {
+      for (int sh = 0; sh < f->nshot; sh++)
+        for (int c = 0; c < f->nch; c++)
+          for (int q = 0; q < f->nfreq; q++)
+            for (int ir = 0; ir < f->nrec; ir++) {
+              const float2 v = h[(((size_t)sh * f->nfreq + q) * f->nch + c) * f->nrec + ir];
+              const size_t o = (((size_t)sh * f->nch + c) * f->nfreq + q) * f->nrec + ir;
+              dcal[2 * o] = v.x;
+              dcal[2 * o + 1] = v.y;
+            }
+    }
+  }
   emmi_solver_destroy(s);
   return rc;
 }
