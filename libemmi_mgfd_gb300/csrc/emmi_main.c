@@ -819,6 +819,13 @@ int main(int argc, char **argv) {
   if (!getparint("mode", &emf.mode)) emf.mode = 0;
   if (emf.mode < 0 || emf.mode > 2) die("mode must be 0 (modelling), 1 (inversion) or 2 (gradient)", NULL);
   if (!getparint("verb", &emf.verb)) emf.verb = 1;
+  if (emf.mode == 1) { /* checked before any work: do_fwi.c:63 */
+    int method = 0;
+    getparint("method", &method);
+    if (method != 0)
+      die("method=1 (Gauss-Newton) needs a Hessian-vector product; the reference's is empty "
+          "(src/fg_fwi.c:316-320): use method=0", NULL);
+  }
   /* ---- emf_init (src/emf_init_free.c:12-128) ---- */
   if (!(emf.nfreq = countparval("freqs"))) die("Need freqs= vector", NULL);
   emf.freqs = malloc(emf.nfreq * sizeof(float));

@@ -64,3 +64,14 @@ def test_create_refuses_grids_beyond_32_bit_offsets(built):
     x = [np.arange(v + 1, dtype=np.float32) for v in n]
     with pytest.raises(G.EmmiError, match="2\\^31"):
         G.Solver(n, *x, np.zeros((1, 4, 1), np.float32), np.ones(1, np.float32))
+
+
+@pytest.mark.parametrize("args,msg", [(["mode=3"], "mode must be"),
+                                      (["mode=1", "method=1"], "Gauss-Newton")])
+def test_main_refuses_bad_parameters_before_any_work(built, tmp_path, args, msg):
+    """emmi_main checks mode= and the inversion method before it reads a
+    file or touches the device, so this runs without a GPU."""
+    import subprocess
+    r = subprocess.run([os.path.join(PKG, "emmi_main")] + args + ["freqs=1"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and msg in (r.stdout + r.stderr), r.stdout + r.stderr
