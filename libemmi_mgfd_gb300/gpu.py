@@ -463,8 +463,9 @@ class Fg:
     Survey (sources, receivers, pairs, channels, frequencies); dobs complex64
     and delta float32 [nshot, nrec_ch, nfreq, nrec]; bathy [ny, nx]."""
 
-    def __init__(self, model, survey, dobs, delta, bathy, options: Optional[Options] = None,
-                 idxpar=(1, 2), preco: int = 1, dsmute: float = 800.0, drmute: float = 200.0):
+    def __init__(self, model, survey, dobs=None, delta=None, bathy=None,
+                 options: Optional[Options] = None, idxpar=(1, 2), preco: int = 1,
+                 dsmute: float = 800.0, drmute: float = 200.0):
         opts = (options or Options())._c()
         xx, yy, zz, _ = model.padded()
         src = np.asarray(survey.sources, np.float32).copy()
@@ -482,6 +483,8 @@ class Fg:
         self.nshot, self.nrec, self.npar, self.preco = nshot, nrec, len(idxpar), preco
         self.nch, self.nfreq = len(survey.chrec), len(survey.freqs)
         self.nxyz = (model.nz, model.ny, model.nx)
+        self.forward_only = dobs is None
+        shp = (nshot, self.nch, self.nfreq, nrec)
         keep = dict(
             omega=(2 * np.pi * np.asarray(survey.freqs, np.float64)).astype(np.float32),
             x1=np.stack([a["x1"] for a in ax]), x2=np.stack([a["x2"] for a in ax]),
@@ -489,19 +492,24 @@ class Fg:
             src_ch=np.array([CHANNELS[c] for c in survey.chsrc], np.int32),
             rec_ch=np.array([CHANNELS[c] for c in survey.chrec], np.int32),
             nrec_shot=np.array([len(r) for r in recs], np.int32), src=src, rec=rec,
-            dobs=np.ascontiguousarray(dobs, np.complex64).reshape(nshot, self.nch, self.nfreq,
-                                                                    nrec),
-            delta=np.ascontiguousarray(delta, np.float32).reshape(nshot, self.nch, self.nfreq,
-                                                                  nrec),
-            idxpar=np.array(idxpar, np.int32), bathy=np.ascontiguousarray(bathy, np.float32))
+            dobs=None if dobs is None else np.ascontiguousarray(dobs, np.complex64).reshape(shp),
+            delta=None if delta is None else np.ascontiguousarray(delta, np.float32).reshape(shp),
+            idxpar=np.array(idxpar, np.int32),
+            bathy=None if bathy is None else np.ascontiguousarray(bathy, np.float32))
+        if self.forward_only:
+            self.npar = 0
+
+        def ptr(a):
+            return None if a is None else _p(a)
         P = _FgProblem(model.nx, model.ny, model.nz, (C.c_float * 3)(model.ox, model.oy, model.oz),
                        (C.c_float * 3)(model.dx, model.dy, model.dz), model.n1, model.n2,
                        model.n3, nshot, self.nfreq, _p(keep["omega"]), _p(keep["x1"]),
                        _p(keep["x2"]), _p(keep["x3"]), model.rho_water(), len(keep["src_ch"]),
                        _p(keep["src_ch"]), self.nch, _p(keep["rec_ch"]), nrec,
-                       _p(keep["nrec_shot"]), _p(src), _p(rec), _p(keep["dobs"]),
-                       _p(keep["delta"]), self.npar, _p(keep["idxpar"]), preco,
-                       _p(keep["bathy"]), dsmute, drmute)
+                       _p(keep["nrec_shot"]), _p(src), _p(rec), ptr(keep["dobs"]),
+                       ptr(keep["delta"]), self.npar,
+                       None if self.forward_only else _p(keep["idxpar"]), preco,
+                       ptr(keep["bathy"]), dsmute, drmute)
         h = C.c_void_p()
         _check(lib().emmi_fg_create(C.byref(h), C.byref(P), C.byref(opts)), "emmi_fg_create")
         self._h = h
@@ -538,6 +546,17 @@ class Fg:
                                    "adjoint_sources", "adjoint_solves", "gradient_out"),
                                   [round(v, 2) for v in ph]))
         return fcost, grad, phess, dcal, rmse, cyc
+
+    def forward(self, model):
+        """(dcal complex64 [nshot, nch, nfreq, nrec], cycles [nshot * nfreq]):
+        forward modelling of every shot and frequency in one solver
+        (emmi_fg_forward) at the resistivities of model."""
+        xx, yy, zz, pad = model.padded()
+        dcal = np.zeros((self.nshot, self.nch, self.nfreq, self.nrec), np.complex64)
+        stats = (_Stats * (self.nshot * self.nfreq))()
+        _check(lib().emmi_fg_forward(self._h, len(xx) - 1, len(yy) - 1, len(zz) - 1, _p(xx),
+                                     _p(yy), _p(zz), _p(pad), _p(dcal), stats), "emmi_fg_forward")
+        return dcal, np.array([s.cycles for s in stats])
 
     def close(self):
         if getattr(self, "_h", None):

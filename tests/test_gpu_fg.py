@@ -123,3 +123,24 @@ def test_gradient_matches_finite_differences():
     print("cosine", cos)
     assert (ratio > 0.5).all() and (ratio < 2.0).all(), ratio
     assert cos >= 0.95, cos
+
+
+@gpu
+def test_fg_forward_matches_reference(golden):
+    """Forward modelling through the batched object without observed data
+    (gpu.Fg(...).forward, emmi_fg_forward) against the reference's receiver
+    data on the layered case; an evaluation on it is refused."""
+    from libemmi_mgfd_gb300 import gpu as G
+    from test_gpu_solver import receiver_parity
+    g = golden("tiny_layered")
+    s = W.tiny_layered()
+    m = host.Model.from_survey(s)
+    f = G.Fg(m, s, options=G.Options(precision=G.PREC_FP64, tol=1e-10, ncycle=120))
+    dcal, cyc = f.forward(m)
+    with pytest.raises(G.EmmiError, match="without observed data"):
+        f.eval(m)
+    f.close()
+    assert (cyc > 0).all()
+    ch = list(s.chrec)
+    amp, ph = receiver_parity(dcal[0, :, 0, :], g["dcal"], ch)
+    assert amp < 1e-4 and ph < 0.05, (amp, ph)
