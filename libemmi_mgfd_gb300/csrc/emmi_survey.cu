@@ -922,8 +922,8 @@ int emmi_fg_create(emmi_fg** out, const emmi_fg_problem* P, const emmi_options* 
       !f->alloc(&f->d_delta, nper) || !f->alloc(&f->d_skin, P->nfreq) ||
       !f->alloc(&f->d_rmse, nper) || !f->alloc(&f->d_term, nper) ||
       !f->alloc(&f->d_fcost, P->nshot) || !f->alloc(&f->d_rho11, f->nxyz) ||
-      !f->alloc(&f->d_rho33, f->nxyz) || !f->alloc(&f->d_grad, (size_t)P->npar * f->nxyz) ||
-      !f->alloc(&f->d_phess, (size_t)P->npar * f->nxyz) ||
+      !f->alloc(&f->d_rho33, f->nxyz) || !f->alloc(&f->d_grad, (size_t)f->npar * f->nxyz) ||
+      !f->alloc(&f->d_phess, (size_t)f->npar * f->nxyz) ||
       !f->alloc(&f->d_cells, (size_t)P->nshot * 4 * f->nc) || !f->alloc(&f->d_dobs, nper) ||
       !f->alloc(&f->d_dcal, nrd) || !f->alloc(&f->d_dres, nrd) || !f->alloc(&f->d_dsyn, nper) ||
       !f->alloc(&f->d_Ef, ne) || !f->alloc(&f->d_Ea, ne) || !f->alloc(&f->d_bm, bm.size()) ||
