@@ -75,3 +75,17 @@ def test_main_refuses_bad_parameters_before_any_work(built, tmp_path, args, msg)
     r = subprocess.run([os.path.join(PKG, "emmi_main")] + args + ["freqs=1"], cwd=tmp_path,
                        capture_output=True, text=True, timeout=60)
     assert r.returncode != 0 and msg in (r.stdout + r.stderr), r.stdout + r.stderr
+
+
+def test_main_refuses_a_truncated_model_file(built, tmp_path):
+    """A model file shorter than nx*ny*nz floats stops emmi_main with an
+    error naming the file, before any device work (no GPU needed)."""
+    import subprocess
+    from libemmi_mgfd_gb300 import workloads as W
+    s = W.tiny_layered()
+    s.write(str(tmp_path))
+    f = tmp_path / "frho11"
+    f.write_bytes(f.read_bytes()[:-4])
+    r = subprocess.run([os.path.join(PKG, "emmi_main")] + s.params(str(tmp_path)), cwd=tmp_path,
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "frho11" in (r.stdout + r.stderr), r.stdout + r.stderr
