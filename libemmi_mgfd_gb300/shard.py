@@ -48,3 +48,25 @@ def allreduce_sum(arrays, pg=None):
         pg.all_reduce(t, op=pg.ReduceOp.SUM)
         out.append(a)
     return out
+
+
+class ShardedObjective:
+    """The data part of fg_fwi over ranks: this rank's evaluator (gpu.Fg
+    built over shots_of_rank's shots, or anything with the same eval)
+    computes its shots' misfits, gradient and pseudo-Hessian in one device
+    pass, and the partial sums are added over the ranks once -- the
+    reference's MPI_Allreduce of the misfit, the pseudo-Hessian and the
+    gradient (src/fg_fwi.c:231, 265, 268).  Every rank returns the same
+    totals: (fcost_dat, grad, phess)."""
+
+    def __init__(self, evaluator, pg=None):
+        self.ev = evaluator
+        self.pg = pg
+
+    def __call__(self, model):
+        fcost, grad, phess = self.ev.eval(model)[:3]
+        f = np.zeros(1, np.float32)
+        for v in np.asarray(fcost, np.float32):  # the shots in order, as the reference sums
+            f[0] = np.float32(f[0] + v)
+        f, grad, phess = allreduce_sum([f, grad, phess], self.pg)
+        return float(f[0]), grad, phess

@@ -8,7 +8,7 @@ import socket
 import numpy as np
 import pytest
 
-from libemmi_mgfd_gb300.shard import allreduce_sum, shots_of_rank
+from libemmi_mgfd_gb300.shard import ShardedObjective, allreduce_sum, shots_of_rank
 
 
 def _free_port():
@@ -101,3 +101,54 @@ def test_a_failed_rank_makes_the_reduction_fail_not_hang(tmp_path):
     # rank 0 either sees the peer's exit as an error or times out: no result
     assert (tmp_path / "r0.err").exists()
     assert not (tmp_path / "r0.npz").exists()
+
+
+class _FakeFg:
+    """Stands in for gpu.Fg on CPU ranks: each shot's misfit, gradient and
+    pseudo-Hessian are seeded by its shot number and scaled by the model."""
+
+    def __init__(self, shots, shape=(2, 5, 6, 7)):
+        self.shots, self.shape = list(shots), shape
+
+    def eval(self, model):
+        fc, g, h = [], np.zeros(self.shape, np.float32), np.zeros(self.shape, np.float32)
+        for s in self.shots:
+            rng = np.random.default_rng(2000 + s)
+            fc.append(np.float32(model * rng.uniform(1.0, 3.0)))
+            g += np.float32(model) * rng.standard_normal(self.shape).astype(np.float32)
+            h += rng.uniform(0.0, 1.0, self.shape).astype(np.float32)
+        return np.array(fc, np.float32), g, h
+
+
+def _objective_rank(rank, world, port, nshots, out):
+    import torch.distributed as D
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    D.init_process_group("gloo", rank=rank, world_size=world,
+                         timeout=datetime.timedelta(seconds=10))
+    try:
+        obj = ShardedObjective(_FakeFg(shots_of_rank(nshots, rank, world)), D)
+        f, g, h = obj(1.5)
+        np.savez(os.path.join(out, f"o{rank}.npz"), f=f, g=g, h=h)
+    finally:
+        D.destroy_process_group()
+
+
+def test_sharded_objective_sums_over_two_gloo_ranks(tmp_path):
+    """The per-rank objective (this rank's shots in one evaluation, then one
+    reduction) gives every rank the all-shot totals."""
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    ps = [ctx.Process(target=_objective_rank, args=(r, 2, port, 5, str(tmp_path)))
+          for r in range(2)]
+    for p in ps:
+        p.start()
+    for p in ps:
+        p.join(120)
+        assert not p.is_alive() and p.exitcode == 0
+    f1, g1, h1 = ShardedObjective(_FakeFg(range(1, 6)))(1.5)
+    for r in range(2):
+        d = np.load(tmp_path / f"o{r}.npz")
+        assert abs(float(d["f"]) - f1) <= 1e-6 * abs(f1)
+        np.testing.assert_allclose(d["g"], g1, rtol=1e-5, atol=1e-5)
+        np.testing.assert_allclose(d["h"], h1, rtol=1e-5, atol=1e-5)
