@@ -505,7 +505,7 @@ def main():
                "sample": sample}
 
     fwi = None
-    if rank == 0 and not a.no_fwi:
+    if rank == 0 and world == 1 and not a.no_fwi:  # a one-GPU figure, like cpu_baseline
         fwi = fwi_eval_bench(a.n, a.tol)
 
     if rank == 0:
