@@ -1,0 +1,42 @@
+"""The Python ctypes mirrors of the C ABI's structs have the C layout: a
+small C program built against include/emmi_gpu.h prints every field's
+offset and each struct's size, compared with ctypes (no GPU)."""
+import ctypes as C
+import os
+import subprocess
+
+import pytest
+
+from libemmi_mgfd_gb300 import gpu as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+STRUCTS = {"emmi_options": G._Options, "emmi_problem": G._Problem,
+           "emmi_survey": G._Survey, "emmi_fg_problem": G._FgProblem,
+           "emmi_rhs_stats": G._Stats}
+
+
+@pytest.fixture(scope="module")
+def c_layout(tmp_path_factory):
+    d = tmp_path_factory.mktemp("layout")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "emmi_gpu.h"',
+             "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = d / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = d / "layout"
+    subprocess.run(["gcc", "-std=gnu99", "-I" + os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {tuple(l.split()[:2]): int(l.split()[2]) for l in out.splitlines()}
+
+
+@pytest.mark.parametrize("cname", sorted(STRUCTS))
+def test_ctypes_mirror_matches_the_c_struct(c_layout, cname):
+    py = STRUCTS[cname]
+    assert C.sizeof(py) == c_layout[(cname, "size")], cname
+    for fname, _ in py._fields_:
+        assert getattr(py, fname).offset == c_layout[(cname, fname)], (cname, fname)
