@@ -1,6 +1,7 @@
 """The Python ctypes mirrors of the C ABI's structs have the C layout: a
-small C program built against include/emmi_gpu.h prints every field's
-offset and each struct's size, compared with ctypes (no GPU)."""
+small C program built against include/emmi_gpu.h and include/emmi_fwi.h
+prints every field's offset and each struct's size, compared with ctypes
+(no GPU)."""
 import ctypes as C
 import os
 import subprocess
@@ -8,18 +9,19 @@ import subprocess
 import pytest
 
 from libemmi_mgfd_gb300 import gpu as G
+from test_fwi_host import EfOpt
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 STRUCTS = {"emmi_options": G._Options, "emmi_problem": G._Problem,
            "emmi_survey": G._Survey, "emmi_fg_problem": G._FgProblem,
-           "emmi_rhs_stats": G._Stats}
+           "emmi_rhs_stats": G._Stats, "ef_opt": EfOpt}
 
 
 @pytest.fixture(scope="module")
 def c_layout(tmp_path_factory):
     d = tmp_path_factory.mktemp("layout")
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "emmi_gpu.h"',
-             "int main(void) {"]
+             '#include "emmi_fwi.h"', "int main(void) {"]
     for cname, py in STRUCTS.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
         for fname, _ in py._fields_:
