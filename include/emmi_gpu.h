@@ -382,9 +382,14 @@ int emmi_level_smooth(const int n[3], const double *x1, const double *x2,
  *   x1..x3 host node coordinates (n_d+1 each); stream may be NULL
  * Levels whose sweep needs more scratch than the maximum, or with n_d
  * outside [2, EMMI_NOALLOC_MAX_N], return EMMI_EINVAL (see emmi_last_error).
- * The first call on a device looks up the array's address on that device;
- * make it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race, calls ordered on one stream do not. */
+ * CUDA loads device code lazily by default, so the array is reserved on a
+ * device by the first call there: make one call on each device before the
+ * caller's pool takes its HBM (or set CUDA_MODULE_LOADING=EAGER); later calls
+ * reserve nothing.  The first call also looks up the array's address on that
+ * device and keeps it: do not use the call across cudaDeviceReset.  Each call
+ * stages the geometry from host memory, so a call on a stream that is being
+ * captured is refused with EMMI_EINVAL.  All calls share the array: calls
+ * that overlap on the GPU race, calls ordered on one stream do not. */
 #define EMMI_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define EMMI_NOALLOC_MAX_N 1024
 int emmi_level_line_sweep_noalloc(const int n[3], const double *x1,

@@ -19,6 +19,10 @@ extern "C" {
 #define EH_ESEARCH -2 /* the reference's source-depth search would read past
                          the padded z axis (src/regrid_init_free.c:194 sizes
                          it by nx); the reference's result is undefined there */
+#define EH_ENUGRID -3 /* a stretched axis has no geometric ratio: the
+                         reference's fixed-point loop (src/create_nugrid.c:
+                         24-31) never ends there, e.g. one cell left below
+                         the source for the bottom stretch (n3 too small) */
 
 typedef struct {
   int nx, ny, nz;           /* input model cells                         */
@@ -40,7 +44,8 @@ typedef struct {
 } eh_grid;
 
 /* create_nugrid.c:13-36: x[0..n] of a geometric progression with first cell
- * dx spanning len; returns the ratio (1 for a uniform grid) */
+ * dx spanning len; returns the ratio (1 for a uniform grid), or 0 where the
+ * fixed-point iteration has no fixed point (the reference never returns) */
 float eh_create_nugrid(int n, float len, float dx, float *x);
 
 /* find_index.c:9-30 */

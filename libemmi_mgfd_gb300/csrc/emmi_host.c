@@ -22,13 +22,24 @@ float eh_create_nugrid(int n, float len, float dx, float *x) {
     return 1;
   }
   /* ratio q with dx (q^n - 1)/(q - 1) = len by fixed-point iteration in
-   * float, each step evaluated in double (create_nugrid.c:24-33) */
+   * float, each step evaluated in double (create_nugrid.c:24-33).  The
+   * reference loops until two iterates are equal; where the iteration has
+   * no fixed point (n = 1 and len > dx: q runs off to infinity, then NaN)
+   * it never returns.  Here the loop is capped and that case returns 0. */
   float q = 1.1f, qq;
   const float eps = 1e-15f;
+  int done = 0;
   for (int it = 0; it < 100000; it++) {
     qq = pow(len * (q - 1.) / dx + 1., 1. / n);
-    if (fabs(qq - q) < eps) break;
+    if (fabs(qq - q) < eps) {
+      done = 1;
+      break;
+    }
     q = qq;
+  }
+  if (!done || !isfinite(q)) {
+    for (int i = 0; i <= n; i++) x[i] = i * dx;
+    return 0;
   }
   x[0] = 0;
   for (int i = 1; i <= n; i++) x[i] = (pow(q, i) - 1.) * dx / (q - 1.);
@@ -132,27 +143,29 @@ float eh_rho_water(const eh_model *m) {
 
 /* padded axis: nb geometric cells on each side of n uniform cells
  * (regrid_init_free.c:47-70) */
-static void padded_axis(int n, float d, float o, int nb, float lextend, float *ax) {
+static int padded_axis(int n, float d, float o, int nb, float lextend, float *ax) {
   float *x = malloc((nb + 1) * sizeof(float));
   for (int i = 0; i <= n; i++) ax[i + nb] = o + i * d;
-  eh_create_nugrid(nb, lextend, d, x);
+  const float q = eh_create_nugrid(nb, lextend, d, x);
   for (int i = 0; i <= nb; i++) {
     ax[i] = o - x[nb - i];
     ax[i + n + nb] = o + n * d + x[i];
   }
   free(x);
+  return q == 0 ? EH_ENUGRID : EH_OK;
 }
 
 /* stretched mesh axis centred on the source: n/2 cells to the low side and
  * the rest to the high side (regrid_init_free.c:156-187) */
-static void centred_axis(int n, float src, float lo, float hi, float dmin, float *out) {
+static int centred_axis(int n, float src, float lo, float hi, float dmin, float *out) {
   const int np1 = n / 2, np2 = n - np1;
   float *x = malloc((n + 1) * sizeof(float));
-  eh_create_nugrid(np1, src - lo, dmin, x);
+  const float q1 = eh_create_nugrid(np1, src - lo, dmin, x);
   for (int i = 0; i <= np1; i++) out[np1 - i] = src - x[i];
-  eh_create_nugrid(np2, hi - src, dmin, x);
+  const float q2 = eh_create_nugrid(np2, hi - src, dmin, x);
   for (int i = 0; i <= np2; i++) out[np1 + i] = src + x[i];
   free(x);
+  return (q1 == 0 || q2 == 0) ? EH_ENUGRID : EH_OK;
 }
 
 int eh_pad_dims(const eh_model *m, int *nxp, int *nyp, int *nzp) {
@@ -170,9 +183,10 @@ int eh_pad_model(const eh_model *m, float *xx, float *yy, float *zz, float *pad)
   int nxp, nyp, nzp;
   if (eh_pad_dims(m, &nxp, &nyp, &nzp) != EH_OK) return EH_EINVAL;
   const int nb = m->nb;
-  padded_axis(m->nx, m->dx, m->ox, nb, m->lextend, xx);
-  padded_axis(m->ny, m->dy, m->oy, nb, m->lextend, yy);
-  padded_axis(m->nz, m->dz, m->oz, nb, m->lextend, zz);
+  if (padded_axis(m->nx, m->dx, m->ox, nb, m->lextend, xx) != EH_OK ||
+      padded_axis(m->ny, m->dy, m->oy, nb, m->lextend, yy) != EH_OK ||
+      padded_axis(m->nz, m->dz, m->oz, nb, m->lextend, zz) != EH_OK)
+    return EH_ENUGRID;
   const size_t np = (size_t)nxp * nyp * nzp;
 #define PAD(a, i, j, k) pad[(size_t)(a) * np + (i) + (size_t)nxp * ((j) + (size_t)nyp * (k))]
   for (int k = 0; k < m->nz; k++)
@@ -212,8 +226,9 @@ int eh_regrid_axes(const eh_model *m, const float *xx, const float *yy, const fl
   int nxp, nyp, nzp;
   if (!g || eh_pad_dims(m, &nxp, &nyp, &nzp) != EH_OK || m->n1 < 2 || m->n2 < 2 || m->n3 < 2)
     return EH_EINVAL;
-  centred_axis(m->n1, sx, xx[0], xx[nxp], m->d1min, g->x1);
-  centred_axis(m->n2, sy, yy[0], yy[nyp], m->d2min, g->x2);
+  if (centred_axis(m->n1, sx, xx[0], xx[nxp], m->d1min, g->x1) != EH_OK ||
+      centred_axis(m->n2, sy, yy[0], yy[nyp], m->d2min, g->x2) != EH_OK)
+    return EH_ENUGRID;
   /* z: input-model nodes down to 5 cells below the source, then stretched
    * to the bottom (regrid_init_free.c:190-205).  The reference sizes the
    * source search by nx (its line 194); it is reproduced, with a check that
@@ -224,9 +239,10 @@ int eh_regrid_axes(const eh_model *m, const float *xx, const float *yy, const fl
   if (np1 > nzp || np2 < 1) return EH_EINVAL;
   for (int i = 0; i <= np1; i++) g->x3[i] = zz[i];
   float *x = malloc((np2 + 1) * sizeof(float));
-  eh_create_nugrid(np2, zz[nzp] - g->x3[np1], m->d3min, x);
+  const float q = eh_create_nugrid(np2, zz[nzp] - g->x3[np1], m->d3min, x);
   for (int i = 0; i <= np2; i++) g->x3[np1 + i] = g->x3[np1] + x[i];
   free(x);
+  if (q == 0) return EH_ENUGRID;
   eh_stagger(m->n1, g->x1, g->x1s, g->d1, g->d1s);
   eh_stagger(m->n2, g->x2, g->x2s, g->d2, g->d2s);
   eh_stagger(m->n3, g->x3, g->x3s, g->d3, g->d3s);

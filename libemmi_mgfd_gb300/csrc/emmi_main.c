@@ -248,7 +248,11 @@ static void set_shot(fg_ctx *c, shot_t *t) {
   eh_grid G = {emf->x1, emf->x2, emf->x3, emf->x1s, emf->x2s, emf->x3s,
                emf->d1, emf->d2, emf->d3, emf->d1s, emf->d2s, emf->d3s,
                c->s11, c->s22, c->s33, c->imu};
-  if (eh_regrid(c->M, t->src5[0], t->src5[1], t->src5[2], &G) != EH_OK) die("regrid failed", NULL);
+  const int rg = eh_regrid(c->M, t->src5[0], t->src5[1], t->src5[2], &G);
+  if (rg == EH_ENUGRID)
+    die("no geometric stretching ratio for a mesh axis (too few cells left below the source "
+        "for the bottom stretch? raise n3)", NULL);
+  if (rg != EH_OK) die("regrid failed", NULL);
 }
 
 /* rmse_%04d.txt of a shot: rmse [nchrec][nfreq][nrec] (write_rmse,
@@ -376,9 +380,12 @@ static void fg_batch_init(fg_ctx *c, int with_data) {
       *rest[k] = q;
       q += len[k % 3];
     }
-    if (eh_regrid_axes(c->M, c->pxx, c->pyy, c->pzz, t->src5[0], t->src5[1], t->src5[2], &g) !=
-        EH_OK)
-      die("eh_regrid_axes failed", NULL);
+    const int rg = eh_regrid_axes(c->M, c->pxx, c->pyy, c->pzz, t->src5[0], t->src5[1],
+                                  t->src5[2], &g);
+    if (rg == EH_ENUGRID)
+      die("no geometric stretching ratio for a mesh axis (too few cells left below the source "
+          "for the bottom stretch? raise n3)", NULL);
+    if (rg != EH_OK) die("eh_regrid_axes failed", NULL);
     memcpy(src + (size_t)is * 5, t->src5, 5 * sizeof(float));
     nrs[is] = t->nrec;
     for (int ir = 0; ir < t->nrec; ir++) {

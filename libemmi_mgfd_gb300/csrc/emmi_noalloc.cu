@@ -11,22 +11,34 @@
 // its own device memory and only needs the sweep.
 //
 // Contract:
-//  * the scratch array is EMMI_NOALLOC_SCRATCH_BYTES per GPU; every GPU that
-//    loads this library holds it until the process exits;
+//  * the scratch array is EMMI_NOALLOC_SCRATCH_BYTES per GPU.  CUDA loads a
+//    library's device code lazily by default (CUDA_MODULE_LOADING=LAZY), so
+//    the array is reserved on a device by the first call there, not when the
+//    library is loaded: make one call on each device before the caller's
+//    pool reserves its HBM, or run with CUDA_MODULE_LOADING=EAGER.  From then
+//    on the device holds the array until the process exits and no call
+//    reserves anything more;
 //  * the first call on a device looks up the array's device address for that
-//    device (cudaGetSymbolAddress, with that device current) and keeps it;
-//    make that first call before any stream capture;
+//    device (cudaGetSymbolAddress, with that device current) and keeps it for
+//    the life of the process: do not use the call across cudaDeviceReset,
+//    which unloads the module the address belongs to;
+//  * each call stages the level's geometry from host memory with
+//    cudaMemcpyAsync; a call on a stream that is being captured is refused
+//    with EMMI_EINVAL, because the copy's host source does not outlive the
+//    call;
 //  * every call on a device shares the one array and leaves its contents
 //    behind; nothing in it needs to start at zero (the assemble launch writes
 //    every record the solve then reads), and two calls whose work overlaps on
 //    the GPU (different streams, no ordering between them) race on it;
 //  * a level whose sweep needs more scratch than the maximum is rejected with
 //    EMMI_EINVAL and a message naming the bytes needed;
-//  * no cudaMalloc, cudaFree or other allocating routine is called.
+//  * no cudaMalloc, cudaFree or other allocating routine is called; the host
+//    staging arrays are ordinary heap memory sized to the level.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "emmi_solver_impl.cuh"
 
@@ -47,7 +59,7 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 // node coordinates x[0..n] -> staggered spacings, the same arithmetic as the
 // solver's set-up: ds (primary spacing, last one mirrored), d (dual spacing)
 void stagger_axis(int n, const double* x, double* d, double* ds) {
-  double xs[kMaxN + 1];
+  std::vector<double> xs(n + 1);
   for (int i = 0; i < n; i++) {
     ds[i] = x[i + 1] - x[i];
     xs[i] = 0.5 * (x[i] + x[i + 1]);
@@ -103,16 +115,27 @@ int sweep_noalloc(const int n[3], const double* const xin[3], const void* cells,
   int rc = scratch_on_current_device(&base);
   if (rc != EMMI_OK) return rc;
 
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) {
+    set_err("emmi_level_line_sweep_noalloc: cudaStreamIsCapturing: %s", cudaGetErrorString(e));
+    return EMMI_ECUDA;
+  }
+  if (cap != cudaStreamCaptureStatusNone) {
+    set_err("emmi_level_line_sweep_noalloc: the stream is being captured; the call stages its "
+            "geometry from host memory that does not outlive the call");
+    return EMMI_EINVAL;
+  }
+
   // geometry rows: 0-2 node coordinates, 3-5 primary spacings, 6-8 dual spacings
-  T g[9 * (kMaxN + 1)];
-  double d[kMaxN + 1], ds[kMaxN + 1];
-  std::fill(g, g + gstride, (T)0);
-  for (int e = 0; e < 3; e++) {
-    stagger_axis(n[e], xin[e], d, ds);
-    for (int i = 0; i <= n[e]; i++) {
-      g[e * gmax1 + i] = (T)xin[e][i];
-      g[(3 + e) * gmax1 + i] = (T)ds[i];
-      g[(6 + e) * gmax1 + i] = (T)d[i];
+  std::vector<T> g((size_t)gstride, (T)0);
+  std::vector<double> d(gmax1), ds(gmax1);
+  for (int ax = 0; ax < 3; ax++) {
+    stagger_axis(n[ax], xin[ax], d.data(), ds.data());
+    for (int i = 0; i <= n[ax]; i++) {
+      g[ax * gmax1 + i] = (T)xin[ax][i];
+      g[(3 + ax) * gmax1 + i] = (T)ds[i];
+      g[(6 + ax) * gmax1 + i] = (T)d[i];
     }
   }
   const T wmu = (T)(omega * kMu0);
@@ -120,7 +143,7 @@ int sweep_noalloc(const int n[3], const double* const xin[3], const void* cells,
   T* dwmu = reinterpret_cast<T*>(base + geo_bytes);
   C_t<T>* drec = reinterpret_cast<C_t<T>*>(base + geo_bytes + 256);
   // pageable sources: each copy returns once g / wmu have been staged
-  cudaError_t e = cudaMemcpyAsync(dgeo, g, (size_t)gstride * sizeof(T), cudaMemcpyHostToDevice, st);
+  e = cudaMemcpyAsync(dgeo, g.data(), (size_t)gstride * sizeof(T), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dwmu, &wmu, sizeof(T), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) {
     set_err("emmi_level_line_sweep_noalloc: geometry upload: %s", cudaGetErrorString(e));

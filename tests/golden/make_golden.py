@@ -10,6 +10,7 @@ GPU machines; these fixtures carry its outputs there.
     python tests/golden/make_golden.py            (needs oracle/_ref built)
     python tests/golden/make_golden.py tiny_grad  (the mode=2 gradient case only)
     python tests/golden/make_golden.py tiny_fwi   (the mode=1 inversion case only)
+    python tests/golden/make_golden.py c3 c2 c4   (benchmark configurations, minutes each)
 """
 from __future__ import annotations
 
@@ -209,10 +210,129 @@ def sensitivity(niter=2):
                       f"{np.abs(np.log(x) - np.log(rho)).max():.3g}")
 
 
+def _receivers_one(s: W.Survey, shot: int, extra):
+    """ref_dump on one shot; the receiver data, residual history and mesh axes."""
+    d = tempfile.mkdtemp(prefix=f"golden_rx{shot}_")
+    s.write(d)
+    args = ([REF_DUMP] + s.params(d, shot=shot) + [f"dumpdir={d}", "adjoint=0", "verb=1"]
+            + list(extra))
+    r = subprocess.run(args, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout + r.stderr)
+    f32, c64 = np.float32, np.complex64
+    hist = []
+    for line in r.stdout.splitlines():
+        if "gmg_init" in line:
+            hist.append([])
+        elif line.startswith("icycle=") and hist:
+            hist[-1].append(float(line.split("rnorm=")[1]))
+    out = {"dcal": load(d, "dcal", c64), "omegas": load(d, "omegas", f32),
+           "rho_water": load(d, "rho_water", f32), "srcrec": load(d, "srcrec", f32),
+           "x1": load(d, "x1", f32), "x2": load(d, "x2", f32), "x3": load(d, "x3", f32),
+           "cycles": np.array([len(h) - 1 for h in hist], np.int32),
+           "rnorm_last": np.array([h[-1] / h[0] if h else np.nan for h in hist], np.float64)}
+    subprocess.run(["rm", "-rf", d])
+    return out
+
+
+def receivers_case(s: W.Survey, shots, extra, tag):
+    """The reference's receiver data (dcal [nch][nfreq][nrec], complex
+    float) for a few shots of a benchmark configuration at the size it is
+    measured on, one reference process per shot (the reference runs one shot
+    per MPI rank, src/acq_init_free.c:119-140).  Receivers only: the fields
+    at these sizes are hundreds of MB."""
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=len(shots)) as ex:
+        outs = list(ex.map(lambda k: _receivers_one(s, k, extra), shots))
+    rec = {"name": np.array(tag), "params": np.array(" ".join(extra)),
+           "n": np.array(s.n, np.int32), "shots": np.array(shots, np.int32),
+           "chsrc": np.array(",".join(s.chsrc)), "chrec": np.array(",".join(s.chrec))}
+    for k, o in zip(shots, outs):
+        for nm, v in o.items():
+            rec[f"s{k}_{nm}"] = v
+    return rec
+
+
+def gradient_case(true: W.Survey, start: W.Survey, shots, extra, tag):
+    """The reference's mode=2 gradient summed over a few shots: per shot a
+    mode=0 run on the true model writes the observed emf_XXXX.txt, then a
+    mode=2 run on the start model (addnoise=0) writes gradient_dat_Rv/Rh;
+    the per-shot gradients are added in float32 as MPI_Allreduce does
+    (src/fg_fwi.c:265-268; two addends, so the order cannot matter)."""
+    import concurrent.futures as cf
+
+    def one(k):
+        d = tempfile.mkdtemp(prefix=f"golden_g{k}_")
+        true.write(os.path.join(d, "true"))
+        start.write(d)
+        r0 = subprocess.run([REF_MAIN] + true.params(os.path.join(d, "true"), shot=k)
+                            + list(extra), cwd=d, capture_output=True, text=True)
+        if r0.returncode != 0:
+            raise RuntimeError(r0.stdout + r0.stderr)
+        obs = open(os.path.join(d, f"emf_{k:04d}.txt")).read()
+        args = [a for a in start.params(d, shot=k)
+                if not a.startswith("mode=") and not a.startswith("verb=")]
+        args += ["mode=2", "verb=1", "addnoise=0", "npar=2", "idxpar=1,2", "preco=1"] + list(extra)
+        r2 = subprocess.run([REF_MAIN] + args, cwd=d, capture_output=True, text=True)
+        if r2.returncode != 0:
+            raise RuntimeError(r2.stdout + r2.stderr)
+        n = start.nx * start.ny * start.nz
+        g = {nm: np.fromfile(os.path.join(d, "gradient_dat_" + nm), np.float32, n)
+             for nm in ("Rv", "Rh")}
+        fc = [float(l.split("=")[1].split(",")[0]) for l in r2.stdout.splitlines()
+              if l.startswith("fcost_dat=")]
+        subprocess.run(["rm", "-rf", d])
+        return obs, g, fc
+
+    with cf.ThreadPoolExecutor(max_workers=len(shots)) as ex:
+        outs = list(ex.map(one, shots))
+    rec = {"name": np.array(tag), "params": np.array(" ".join(extra)),
+           "n": np.array(start.n, np.int32), "shots": np.array(shots, np.int32)}
+    for nm in ("Rv", "Rh"):
+        acc = np.zeros_like(outs[0][1][nm])
+        for o in outs:
+            acc = (acc + o[1][nm]).astype(np.float32)
+        rec[f"grad_{nm}"] = acc
+    for k, o in zip(shots, outs):
+        rec[f"s{k}_obs_text"] = np.array(o[0])
+        rec[f"s{k}_fcost_dat"] = np.array(o[2], np.float64)
+    return rec
+
+
+def config_cases(which):
+    """Fixtures at the benchmark configurations' sizes (minutes of CPU):
+    c3: two shots of the 128^3 log-normal configuration to 1e-10;
+    c2: two shots x two frequencies of the VTI/bathymetry configuration on a
+        48x48x64 mesh (the reference cannot mesh it with n3 = 40: the source
+        sits 39 input cells down, which leaves one cell for the bottom
+        stretch, and create_nugrid's fixed-point loop never ends there);
+    c4: the mode=2 gradient of the half-space start model against the
+        reservoir model's data, two shots x three frequencies at 64^3."""
+    if which == "c3":
+        s = W.config3(128)
+        rec = receivers_case(s, [1, 13], ["tol=1e-10", "ncycle=200"], "c3_lognormal_128_ref")
+    elif which == "c2":
+        s = W.config2(96)
+        s.n = (48, 48, 64)
+        rec = receivers_case(s, [1, 13], ["tol=1e-10", "ncycle=200"], "c2_vti_48x48x64_ref")
+    else:
+        true = W.config4(64, true_model=True)
+        start = W.config4(64, true_model=False)
+        rec = gradient_case(true, start, [1, 13], ["tol=1e-10", "ncycle=200"],
+                            "c4_reservoir_64_grad_ref")
+    path = os.path.join(HERE, str(rec["name"]) + ".npz")
+    np.savez_compressed(path, **rec)
+    print(rec["name"], os.path.getsize(path) // 1024, "KB")
+
+
 def main():
     if not os.path.exists(REF_DUMP):
         sys.exit("oracle/_ref/ref_dump missing: run `make -C oracle ref` first")
     only = set(sys.argv[1:])
+    if only and only <= {"c2", "c3", "c4"}:
+        for w in sorted(only):
+            config_cases(w)
+        return
     if only == {"sensitivity"}:
         sensitivity()
         return

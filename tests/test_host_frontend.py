@@ -51,3 +51,37 @@ def test_search_past_padded_axis_is_reported():
     m.rho33 = m.rho11
     with pytest.raises(RuntimeError):
         m.regrid(0.0, 0.0, 2100.0)
+
+
+def test_batched_vti_mesh_axes_match_reference(golden):
+    """The 25-shot VTI/bathymetry configuration on the 48x48x64 mesh its
+    reference fixture was made on: both fixture shots' mesh axes bit for
+    bit (the reference's own run, tests/golden/c2_vti_48x48x64_ref.npz)."""
+    g = golden("c2_vti_48x48x64_ref")
+    s = W.config2(96)
+    s.n = tuple(int(v) for v in g["n"])
+    m = host.Model.from_survey(s)
+    xx, yy, zz, _ = m.padded()
+    for k in g["shots"]:
+        src = s.sources[int(k) - 1]
+        ax = m.axes(xx, yy, zz, float(src[0]), float(src[1]), float(src[2]))
+        for nm in ("x1", "x2", "x3"):
+            assert np.array_equal(ax[nm], g[f"s{k}_{nm}"]), (k, nm)
+
+
+def test_mesh_without_a_geometric_ratio_is_reported():
+    """The same configuration on a 40^3 mesh: the source lies 39 padded
+    cells down, one cell is left for the bottom stretch, and the
+    reference's fixed-point loop for its ratio never ends
+    (src/create_nugrid.c:24-31).  The front end reports EH_ENUGRID."""
+    import ctypes as C
+    s = W.config2(40)
+    m = host.Model.from_survey(s)
+    xx, yy, zz, _ = m.padded()
+    src = s.sources[0]
+    with pytest.raises(RuntimeError, match=r"\(-3\)"):
+        m.axes(xx, yy, zz, float(src[0]), float(src[1]), float(src[2]))
+    x = np.zeros(2, np.float32)
+    r = host.lib().eh_create_nugrid(1, C.c_float(5e4), C.c_float(20.0),
+                                    x.ctypes.data_as(C.c_void_p))
+    assert r == 0.0
