@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-parity", action="store_true",
+                   help="skip the receiver parity report (FP64 solve of the batch to 1e-12)")
     p.add_argument("--no-fwi", action="store_true",
                    help="skip the inversion objective evaluation (fwi_eval)")
     p.add_argument("--only-fwi", action="store_true",
@@ -175,13 +177,50 @@ def fwi_eval_bench(n: int, tol: float):
     return out
 
 
-def make_solver(w, precision, tol, krylov=0):
+def parity_report(w, d, a):
+    """Receiver errors of d (the benchmark's solve: [nrhs, nch, nrec]) against
+    an FP64 solve of the same batch to 1e-12 and against the reference's
+    receiver data where a fixture holds them."""
+    from libemmi_mgfd_gb300 import gpu as G
+    from libemmi_mgfd_gb300.parity import receiver_errors
+    s = w["survey"]
+    ch = list(s.chrec)
+    sp = make_solver(w, G.PREC_FP64, 1e-12, ncycle=200)
+    d64, st64, _ = sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+    sp.close()
+    per = [receiver_errors(d[r], d64[r], ch) for r in range(d.shape[0])]
+    out = {"bar": "amplitude <= 1e-4 of the channel scale, phase <= 0.05 deg",
+           "vs_fp64": {"tol": 1e-12,
+                       "all_converged": all(q["status"] == "ok" for q in st64),
+                       "cycles_mean": float(np.mean([q["cycles"] for q in st64])),
+                       "amplitude_max": max(p[0] for p in per),
+                       "phase_deg_max": max(p[1] for p in per),
+                       "per_shot": [[float(f"{p[0]:.3e}"), float(f"{p[1]:.3e}")] for p in per]}}
+    path = os.path.join(ROOT, "tests", "golden", "c3_lognormal_128_ref.npz")
+    if a.n == 128 and d.shape[0] == 25 and os.path.exists(path):
+        g = np.load(path)
+        ref = {"reference_tol": 1e-10, "shots": [], "amplitude": [], "phase_deg": [],
+               "fp64_amplitude": [], "fp64_phase_deg": []}
+        for k in g["shots"]:
+            k = int(k)
+            am, ph = receiver_errors(d[k - 1], g[f"s{k}_dcal"], ch)
+            a64, p64 = receiver_errors(d64[k - 1], g[f"s{k}_dcal"], ch)
+            ref["shots"].append(k)
+            ref["amplitude"].append(float(f"{am:.3e}"))
+            ref["phase_deg"].append(float(f"{ph:.3e}"))
+            ref["fp64_amplitude"].append(float(f"{a64:.3e}"))
+            ref["fp64_phase_deg"].append(float(f"{p64:.3e}"))
+        out["vs_reference"] = ref
+    return out
+
+
+def make_solver(w, precision, tol, krylov=0, ncycle=100):
     from libemmi_mgfd_gb300 import gpu as G
     n = w["survey"].n
     nrhs = w["X1"].shape[0]
     return G.Solver(n, w["X1"], w["X2"], w["X3"], w["cells"], w["omega"],
                     op=np.arange(nrhs, dtype=np.int32),
-                    options=G.Options(precision=precision, tol=tol, ncycle=100, krylov=krylov),
+                    options=G.Options(precision=precision, tol=tol, ncycle=ncycle, krylov=krylov),
                     rho_water=w["rho_water"])
 
 
@@ -259,17 +298,38 @@ def ncu_traffic():
 
 
 # ---------------------------------------------------------------- CPU leg
-def cpu_sample(w, nthreads, cycles_per_solve, ncyc=1):
+def reference_cycles(n: int, tol: float):
+    """F-cycles the reference itself needs to reach tol on this workload:
+    the residual histories it printed solving shots 1 and 13 of the 128^3
+    configuration (tests/golden/c3_lognormal_128_ref.npz, made by running
+    the reference compiled from its sources); None for other sizes."""
+    path = os.path.join(ROOT, "tests", "golden", "c3_lognormal_128_ref.npz")
+    if n != 128 or not os.path.exists(path):
+        return None
+    g = np.load(path)
+    counts = []
+    for k in g["shots"]:
+        h = g[f"s{k}_rnorm_f0"]
+        below = np.nonzero(h / h[0] < tol)[0]
+        if len(below) == 0:
+            return None
+        counts.append(int(below[0]))
+    return float(np.mean(counts)), [int(k) for k in g["shots"]], counts
+
+
+def cpu_sample(w, nthreads, cycles_per_solve, cycles_note):
     """Oracle (the reference's algorithm, lexicographic sweeps) on host
-    threads: each thread one shot, `ncyc` F-cycles including its setup.
-    Returns (solves/s, seconds, sample text)."""
+    threads, one shot per thread, each one F-cycle of its own solve with the
+    set-up before it timed apart.  A solve is the set-up plus
+    `cycles_per_solve` cycles; the batch of `nthreads` concurrent solves
+    takes as long as its slowest thread.  Returns (solves/s, seconds,
+    sample text)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     s = w["survey"]
     n = s.n
     nshots = w["X1"].shape[0]
-    from libemmi_mgfd_gb300 import workloads as W  # noqa: F401
     # right-hand sides by the oracle's restatement of inject_source
     grids = w["grids"]
     bs = []
@@ -281,17 +341,22 @@ def cpu_sample(w, nthreads, cycles_per_solve, ncyc=1):
 
     def one(i):
         g = grids[i % nshots]
-        O.gmg_solve(n, g["x1"], g["x2"], g["x3"], g["sigma11"], g["sigma22"], g["sigma33"],
-                    g["invmur"], float(w["omega"][0]), bs[i], ncycle=ncyc, tol=0.0,
-                    ordering=O.ORDER_LEX)
+        r = O.gmg_solve(n, g["x1"], g["x2"], g["x3"], g["sigma11"], g["sigma22"], g["sigma33"],
+                        g["invmur"], float(w["omega"][0]), bs[i], ncycle=1, tol=0.0,
+                        ordering=O.ORDER_LEX, timing=True)
+        return r[4]
 
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
-        list(ex.map(one, range(nthreads)))
+        tm = list(ex.map(one, range(nthreads)))
     dt = time.perf_counter() - t0
-    value = nthreads * ncyc / (dt * cycles_per_solve)
-    sample = (f"{nthreads} concurrent shots x {ncyc} F-cycle(s) of the {n[0]}^3 system "
-              f"(setup included) in {dt:.1f} s, scaled by {cycles_per_solve:.1f} cycles per solve")
+    per_solve = max(su + cycles_per_solve * cy for su, cy in tm)
+    value = nthreads / per_solve
+    su = max(t[0] for t in tm)
+    cy = max(t[1] for t in tm)
+    sample = (f"{nthreads} concurrent shots of the {n[0]}^3 system, one F-cycle each: set-up "
+              f"{su:.2f} s and {cy:.2f} s per F-cycle (slowest thread); a solve = set-up + "
+              f"{cycles_per_solve:.1f} F-cycles ({cycles_note})")
     return value, dt, sample
 
 
@@ -437,6 +502,13 @@ def main():
             "algorithmic_bytes_per_launch": by / nl, "peak_kind": peak_kind}
     solver.close()
 
+    # parity of the timed step's receiver data: against an FP64 solve of the
+    # same batch to 1e-12 (every shot) and against the reference's own data
+    # for the shots it was run on (tests/golden/c3_lognormal_128_ref.npz)
+    parity = None
+    if not a.no_parity:
+        parity = parity_report(w, d, a)
+
     # e2e: from host arrays through the C ABI, solver setup included
     e2e_times, h2d, d2h = [], 0, 0
     m = w["model"]
@@ -498,9 +570,9 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
-        cps = plain["cycles_mean"] if plain else float(np.mean(cycles))
+        cps, note = ref_cycle_count(a, plain, cycles)
         nthr = os.cpu_count() or 1
-        v, dt, sample = cpu_sample(w, nthr, cps)
+        v, dt, sample = cpu_sample(w, nthr, cps, note)
         cpu = {"value": round(v, 5), "unit": UNIT, "cores": nthr, "kind": "port",
                "sample": sample}
 
@@ -531,10 +603,28 @@ def main():
             "learned": learned, "mixed_without_learned": without,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": round(value / plain["value"], 3) if plain else None,
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fwi_eval": fwi,
+            "roofline": roof, "parity": parity, "cpu_baseline": cpu, "e2e": e2e,
+            "fwi_eval": fwi,
             "gpu_launches": timed_launches, "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
+
+
+def ref_cycle_count(a, plain, cycles):
+    """(F-cycles per solve of the reference's algorithm, where the number
+    comes from): the reference's own count on this configuration, else the
+    FP64 GPU count of the same algorithm (multicolour sweeps)."""
+    rc = reference_cycles(a.n, a.tol)
+    if rc is not None:
+        mean, shots, counts = rc
+        return mean, (f"the reference's own F-cycle count to {a.tol:g} on shots "
+                      f"{', '.join(map(str, shots))} of this configuration: "
+                      f"{', '.join(map(str, counts))}")
+    if plain:
+        return plain["cycles_mean"], "the FP64 GPU count of the same algorithm"
+    if cycles:
+        return float(np.mean(cycles)), "the GPU's cycle count"
+    return 16.0, "the reference's count at 128^3 on the layered model"
 
 
 def reference_arm(a, rank, world, pg):
@@ -546,14 +636,12 @@ def reference_arm(a, rank, world, pg):
     B.build()
     w = build_workload(a.n)
     nthr = os.cpu_count() or 1
-    # cycles per solve of this configuration (reference algorithm, 128^3,
-    # to 1e-8): measured by the FP64 GPU run of the same algorithm
-    cps = float(os.environ.get("EMMI_REF_CYCLES", "7.1"))
+    cps, note = ref_cycle_count(a, None, None)
     for _ in range(max(0, a.warmup)):
-        cpu_sample(w, nthr, cps)
+        cpu_sample(w, nthr, cps, note)
     vals, secs = [], 0.0
     for _ in range(max(1, a.steps)):
-        v, dt, sample = cpu_sample(w, nthr, cps)
+        v, dt, sample = cpu_sample(w, nthr, cps, note)
         vals.append(v)
         secs += dt
     value = statistics.mean(vals)

@@ -84,6 +84,13 @@ typedef struct {
                        process per (grid, RHS, direction); no shape changes
                        any result (1); 0 = default shapes; -k (k = 1..10)
                        forces shape k in every direction (checks)          */
+  int line_sweep;   /* 1 = one launch per colour: each thread assembles,
+                       factors and solves one line, keeping the multipliers
+                       only between its two substitutions (fp16 when
+                       line_factors = 2, else working precision); no stored
+                       factors.  0 = three launches per colour (residual
+                       rows, substitution, update) with the stored factors
+                       of line_factors (default)                          */
 } emmi_options;
 
 typedef struct {
@@ -116,6 +123,10 @@ int emmi_solver_solve(emmi_solver *s, const double *b, double *x, double *h,
 
 /* Seconds of device time of the last solve (CUDA events on its stream). */
 double emmi_solver_last_time(const emmi_solver *s);
+/* Multiplier format of the one-launch line sweep: 1 = fp16, 0 = working
+ * precision (an fp16 multiplier out of range during a solve switches the
+ * solver to 0 and restarts its inner cycles), -1 = the three-launch sweep. */
+int emmi_solver_line_format(const emmi_solver *s);
 /* Number of kernel launches in the last solve. */
 long emmi_solver_last_launches(const emmi_solver *s);
 /* Device bytes held by the solver. */
@@ -202,6 +213,14 @@ int emmi_learned_set(emmi_solver *s, const float *W);
  * level-0 iterates: u += N(D^-1 (f - A u)), f and u device arrays
  * [nrhs][3][S] of the solver's operators (synchronises the stream). */
 int emmi_learned_apply(emmi_solver *s, const void *f, void *u);
+/* Test hook of the convolution's bounded waits (no counterpart in the
+ * reference): the following emmi_learned_apply calls of s give up a wait
+ * after wait_cycles clocks (0: the default, about a second), and with
+ * stall = 1 the producer issues no copy and no MMA, so the first wait of
+ * the epilogue runs out: the kernel records the failure, frees its tensor
+ * memory and returns, and emmi_learned_apply reports EMMI_ECUDA.  Solves
+ * never use these settings. */
+int emmi_learned_wait_hook(emmi_solver *s, long long wait_cycles, int stall);
 
 /* ---- survey: injection, extraction, gradient (src/inject_extract.c,
  *      src/build_gradient.c) ------------------------------------------- */

@@ -1336,6 +1336,354 @@ void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac
   else line_sweep_fac_d<T, 2>(L, color, fac, grp, rb, fmt, sh, st);
 }
 
+// ---------------------------------------------------------------- fused line relaxation
+// One launch per colour and direction.  A thread owns one line and walks it
+// twice:
+//   forward   node by node it assembles each row -- band entries and the
+//             residual of the current iterate, the row arithmetic of
+//             assemble_row -- and feeds it to the streaming LDL^T of
+//             k_line_solve: the arriving row eliminates pivot row-5, whose
+//             z = D^-1 L^-1 r and L(p+i, p), i = 1..5, are set aside;
+//   backward  x_p = z_p - sum_i L(p+i, p) x_{p+i}, u += x at the row's slot.
+// z_p waits in the level's residual buffer at row p's own slot: no other line
+// of the colour reads or writes it, and that buffer is dead while the level
+// smooths (the cycle recomputes the residual after smoothing).  L waits in
+// the line scratch, [row][line] planes per RHS:
+//   kLExact  the T-precision values (k_line_solve's arithmetic, bit for bit
+//            the same operations in the same order);
+//   kLHalf   (T = float) rounded to fp16 and used rounded by both
+//            substitutions while the elimination keeps the unrounded value:
+//            each line solve is then exact for a matrix within fp16 rounding
+//            of the line's -- the arithmetic of the stored-factor format
+//            kFacF16.  An L value outside the fp16 range sets *ovf.
+// Against the three-kernel sweep this writes no band records and reads no
+// stored factors: per row the neighbourhood of the residual, L (20 or 40
+// bytes) and z (8 bytes) out and back, and u read-modify-write.
+template <typename T, int LF> struct LineL;
+template <> struct LineL<float, kLExact> {
+  static constexpr long kBytes = 40;  // per row
+  float4* p0;
+  float4* p1;
+  float2* p2;
+  __device__ __forceinline__ LineL(void* base, int m, long nl) {
+    p0 = reinterpret_cast<float4*>(base);
+    p1 = p0 + (long)m * nl;
+    p2 = reinterpret_cast<float2*>(p1 + (long)m * nl);
+  }
+  __device__ __forceinline__ bool put(long o, const float2 (&l)[6]) {
+    p0[o] = make_float4(l[1].x, l[1].y, l[2].x, l[2].y);
+    p1[o] = make_float4(l[3].x, l[3].y, l[4].x, l[4].y);
+    p2[o] = l[5];
+    return false;
+  }
+  __device__ __forceinline__ void round(float2 (&) [6]) const {}
+  __device__ __forceinline__ void get(long o, float2 (&l)[5]) const {
+    const float4 a = p0[o], b = p1[o];
+    l[0] = make_float2(a.x, a.y);
+    l[1] = make_float2(a.z, a.w);
+    l[2] = make_float2(b.x, b.y);
+    l[3] = make_float2(b.z, b.w);
+    l[4] = p2[o];
+  }
+};
+template <> struct LineL<double, kLExact> {
+  static constexpr long kBytes = 80;
+  double2* p;
+  long ps;
+  __device__ __forceinline__ LineL(void* base, int m, long nl) {
+    p = reinterpret_cast<double2*>(base);
+    ps = (long)m * nl;
+  }
+  __device__ __forceinline__ bool put(long o, const double2 (&l)[6]) {
+#pragma unroll
+    for (int i = 0; i < 5; i++) p[i * ps + o] = l[i + 1];
+    return false;
+  }
+  __device__ __forceinline__ void round(double2 (&) [6]) const {}
+  __device__ __forceinline__ void get(long o, double2 (&l)[5]) const {
+#pragma unroll
+    for (int i = 0; i < 5; i++) l[i] = p[i * ps + o];
+  }
+};
+template <> struct LineL<float, kLHalf> {
+  static constexpr long kBytes = 20;
+  uint4* la;
+  uint32_t* lb;
+  __device__ __forceinline__ LineL(void* base, int m, long nl) {
+    la = reinterpret_cast<uint4*>(base);
+    lb = reinterpret_cast<uint32_t*>(la + (long)m * nl);
+  }
+  // l[1..5] rounded to fp16 in place (the values both substitutions use);
+  // true when one left the fp16 range
+  __device__ __forceinline__ void round(float2 (&l)[6]) const {
+#pragma unroll
+    for (int i = 1; i < 6; i++) l[i] = __half22float2(__floats2half2_rn(l[i].x, l[i].y));
+  }
+  __device__ __forceinline__ bool put(long o, const float2 (&l)[6]) {
+    __half2 h[5];
+    bool over = false;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      h[i] = __floats2half2_rn(l[i + 1].x, l[i + 1].y);
+      over |= !(fabsf(l[i + 1].x) <= 65504.f && fabsf(l[i + 1].y) <= 65504.f);
+    }
+    la[o] = make_uint4(h2u(h[0]), h2u(h[1]), h2u(h[2]), h2u(h[3]));
+    lb[o] = h2u(h[4]);
+    return over;
+  }
+  __device__ __forceinline__ void get(long o, float2 (&l)[5]) const {
+    const uint4 a = la[o];
+    l[0] = u2f2(a.x);
+    l[1] = u2f2(a.y);
+    l[2] = u2f2(a.z);
+    l[3] = u2f2(a.w);
+    l[4] = u2f2(lb[o]);
+  }
+};
+
+long line_l_bytes(const int n[3], int d, int color, int lf, int tsize) {
+  const long m = 5 * n[d] - 4, nl = line_count(n, d, color);
+  const long b = lf == kLHalf ? 20 : (tsize == 8 ? 80 : 40);
+  return (m * nl * b + 255) / 256 * 256;
+}
+
+// band entries (lower, real), diagonal and residual of row type TT of node s
+template <typename T, int D, int TT, int C>
+__device__ __forceinline__ void fused_row(const LevelView<T>& L, const C_t<T>* u, const C_t<T>* f,
+                                          const T* cells, const Geo<T>& G, T wmu, int ta, int tb,
+                                          int s, int row, const long ss[3], C_t<T> (&wrow)[6],
+                                          C_t<T>& r) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  int P[3];
+  P[D] = (TT == 0) ? s - 1 : s;
+  P[A] = ta - (TT == 1 ? 1 : 0);
+  P[B] = tb - (TT == 3 ? 1 : 0);
+  const int sl = P[0] + (L.n[0] + 1) * (P[1] + (L.n[1] + 1) * P[2]);  // 32-bit slot
+  EdgeCoef<T> e;
+  const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
+  r = csub<T>(f[C * (int)L.S + sl], au);
+  T band[5] = {0, 0, 0, 0, 0};
+#define LINE_ENTRY(K)                                                         \
+  {                                                                           \
+    constexpr int off = line_off(D, TT, K);                                   \
+    if constexpr (off < 0) {                                                  \
+      if (row + off >= 0) band[5 + off] = e.c[K];                             \
+    }                                                                         \
+  }
+  LINE_ENTRY(0) LINE_ENTRY(1) LINE_ENTRY(2) LINE_ENTRY(3) LINE_ENTRY(4) LINE_ENTRY(5)
+  LINE_ENTRY(6) LINE_ENTRY(7) LINE_ENTRY(8) LINE_ENTRY(9) LINE_ENTRY(10) LINE_ENTRY(11)
+#undef LINE_ENTRY
+#pragma unroll
+  for (int j = 0; j < 5; j++) wrow[j] = mk<T>(band[j], 0);
+  wrow[5] = mk<T>(e.dre, e.dim);
+}
+
+// one elimination step of the streaming LDL^T (k_line_solve's order): the
+// new row sits in W[WI(5, .)], y[5]; pivot W[0] is eliminated.  Returns
+// z = y_0 / d_0 and the multipliers l[1..5] (rounded by LS::round for kLHalf,
+// the unrounded ones updating the window)
+template <typename T, typename LS>
+__device__ __forceinline__ C_t<T> fused_eliminate(C_t<T> (&W)[21], C_t<T> (&y)[6],
+                                                  C_t<T> (&lr)[6], const LS& ls) {
+  const C_t<T> id = crcp<T>(W[0]);
+  C_t<T> lq[6];
+#pragma unroll
+  for (int i = 1; i < 6; i++) lq[i] = cmul<T>(W[WI(i, 0)], id);
+#pragma unroll
+  for (int i = 1; i < 6; i++) lr[i] = lq[i];
+  ls.round(lr);
+#pragma unroll
+  for (int i = 1; i < 6; i++) {
+#pragma unroll
+    for (int j = 1; j <= i; j++) W[WI(i, j)] = cfms<T>(W[WI(i, j)], lq[i], W[WI(j, 0)]);
+    y[i] = cfms<T>(y[i], lr[i], y[0]);
+  }
+  const C_t<T> z = cmul<T>(y[0], id);
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+#pragma unroll
+    for (int j = 0; j <= i; j++) W[WI(i, j)] = W[WI(i + 1, j + 1)];
+    y[i] = y[i + 1];
+  }
+  return z;
+}
+
+template <typename T, int D, int LF, int NT>
+__global__ void __launch_bounds__(NT) k_line_fused(LevelView<T> L, int pa, int pb, LineDiv dv,
+                                                   void* __restrict__ lbuf, long lstride,
+                                                   int* __restrict__ ovf) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  using LS = LineL<T, LF>;
+  const int rhs = blockIdx.y;
+  if (L.active && !L.active[rhs]) return;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (l >= g.nl) return;
+  const unsigned lq = fdiv((unsigned)l, dv.la);
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
+  const int n0 = L.n[0] + 1, n1 = L.n[1] + 1;
+  const long ss[3] = {1, (long)n0, (long)n0 * n1};
+  C_t<T>* __restrict__ u = L.u + (long)rhs * 3 * L.S;
+  const C_t<T>* __restrict__ f = L.f + (long)rhs * 3 * L.S;
+  C_t<T>* __restrict__ zr = L.r + (long)rhs * 3 * L.S;
+  const T* __restrict__ cells = L.cells + (long)op_of(L, rhs) * 4 * L.ncell;
+  const Geo<T> G{L.geo + (long)op_of(L, rhs) * L.gstride, L.gmax1};
+  const T wmu = L.wmu[rhs];
+  LS ls(static_cast<char*>(lbuf) + (long)rhs * lstride, g.m, g.nl);
+  const int nd = g.nd;
+  bool over = false;
+
+  C_t<T> W[21], y[6], lr[6];
+#pragma unroll
+  for (int i = 0; i < 21; i++) W[i] = mk<T>(0, 0);
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    W[WI(i, i)] = mk<T>(1, 0);  // dummy leading rows
+    y[i] = mk<T>(0, 0);
+  }
+  // Rows are assembled a node at a time -- the five rows' loads issued
+  // together, ahead of the node's five elimination steps -- so a node waits
+  // on memory once rather than once per row.  The arriving row (s, TT)
+  // eliminates pivot (s-1, TT): same row type, one node back; with s = 1 the
+  // pivots are the dummy leading rows.
+  C_t<T> rw[5][6], rr[5];
+  auto assemble = [&](auto tt, int s) {
+    constexpr int TT = decltype(tt)::value;
+    constexpr int C = (TT == 0) ? D : (TT <= 2 ? A : B);
+    fused_row<T, D, TT, C>(L, u, f, cells, G, wmu, ta, tb, s, 5 * (s - 1) + TT, ss, rw[TT],
+                           rr[TT]);
+  };
+  auto arrive = [&](auto tt, int s) {
+    constexpr int TT = decltype(tt)::value;
+#pragma unroll
+    for (int j = 0; j < 6; j++) W[WI(5, j)] = rw[TT][j];
+    y[5] = rr[TT];
+    const C_t<T> z = fused_eliminate<T>(W, y, lr, ls);
+    if (s >= 2) {
+      const int p = 5 * (s - 2) + TT;
+      zr[line_slot<D, TT>(L.n, L.S, ta, tb, s - 1)] = z;
+      over |= ls.put((long)p * g.nl + l, lr);
+    }
+  };
+  // trailing steps: identity rows flush pivots (s, TT) of the last rows
+  auto flush = [&](auto tt, int s) {
+    constexpr int TT = decltype(tt)::value;
+#pragma unroll
+    for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
+    W[WI(5, 5)] = mk<T>(1, 0);
+    y[5] = mk<T>(0, 0);
+    const C_t<T> z = fused_eliminate<T>(W, y, lr, ls);
+    const int p = 5 * (s - 1) + TT;
+    zr[line_slot<D, TT>(L.n, L.S, ta, tb, s)] = z;
+    over |= ls.put((long)p * g.nl + l, lr);
+  };
+  using I0 = std::integral_constant<int, 0>;
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  using I3 = std::integral_constant<int, 3>;
+  using I4 = std::integral_constant<int, 4>;
+  for (int s = 1; s < nd; s++) {
+    assemble(I0{}, s);
+    assemble(I1{}, s);
+    assemble(I2{}, s);
+    assemble(I3{}, s);
+    assemble(I4{}, s);
+    arrive(I0{}, s);
+    arrive(I1{}, s);
+    arrive(I2{}, s);
+    arrive(I3{}, s);
+    arrive(I4{}, s);
+  }
+  assemble(I0{}, nd);
+  arrive(I0{}, nd);
+  flush(I1{}, nd - 1);
+  flush(I2{}, nd - 1);
+  flush(I3{}, nd - 1);
+  flush(I4{}, nd - 1);
+  flush(I0{}, nd);
+  if (over && ovf) atomicOr(ovf, 1);
+
+  // backward: rows m-1 .. 0, i.e. (nd, 0), then (s, 4..0) for s = nd-1 .. 1
+  C_t<T> xw[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) xw[i] = mk<T>(0, 0);
+  // backward a node at a time as well: its rows' multipliers, z and u are
+  // loaded together before the five substitution steps
+  C_t<T> bl[5][5], bz[5], bu[5];
+  long bs[5];
+  auto load = [&](auto tt, int s) {
+    constexpr int TT = decltype(tt)::value;
+    bs[TT] = line_slot<D, TT>(L.n, L.S, ta, tb, s);
+    ls.get((long)(5 * (s - 1) + TT) * g.nl + l, bl[TT]);
+    bz[TT] = zr[bs[TT]];
+    bu[TT] = u[bs[TT]];
+  };
+  auto back = [&](auto tt) {
+    constexpr int TT = decltype(tt)::value;
+    C_t<T> x = bz[TT];
+#pragma unroll
+    for (int i = 0; i < 5; i++) x = cfms<T>(x, bl[TT][i], xw[i]);
+#pragma unroll
+    for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
+    xw[0] = x;
+    u[bs[TT]] = cadd<T>(bu[TT], x);
+  };
+  load(I0{}, nd);
+  back(I0{});
+  for (int s = nd - 1; s >= 1; s--) {
+    load(I4{}, s);
+    load(I3{}, s);
+    load(I2{}, s);
+    load(I1{}, s);
+    load(I0{}, s);
+    back(I4{});
+    back(I3{});
+    back(I2{});
+    back(I1{});
+    back(I0{});
+  }
+}
+
+template <typename T, int D, int LF, int NT>
+static void fused_launch(const LevelView<T>& L, int pa, int pb, long nl, void* lbuf, long lstride,
+                         int* ovf, cudaStream_t st) {
+  const LineDiv dv = line_div<D>(L.n, pa, pb);
+  dim3 g((unsigned)((nl + NT - 1) / NT), L.nrhs);
+  k_line_fused<T, D, LF, NT><<<g, NT, 0, st>>>(L, pa, pb, dv, lbuf, lstride, ovf);
+}
+
+template <typename T, int D>
+static void line_fused_d(const LevelView<T>& L, int color, void* lbuf, int lf, int nt, int* ovf,
+                         cudaStream_t st) {
+  const int pa = color & 1, pb = (color >> 1) & 1;
+  const long nl = line_count(L.n, D, color);
+  if (nl == 0) return;
+  const long lstride = line_l_bytes(L.n, D, color, lf, (int)sizeof(T));
+  if constexpr (std::is_same<T, float>::value) {
+    if (lf == kLHalf) {
+      if (nt == 32) fused_launch<T, D, kLHalf, 32>(L, pa, pb, nl, lbuf, lstride, ovf, st);
+      else if (nt == 128) fused_launch<T, D, kLHalf, 128>(L, pa, pb, nl, lbuf, lstride, ovf, st);
+      else fused_launch<T, D, kLHalf, 64>(L, pa, pb, nl, lbuf, lstride, ovf, st);
+      return;
+    }
+  }
+  if (nt == 32) fused_launch<T, D, kLExact, 32>(L, pa, pb, nl, lbuf, lstride, ovf, st);
+  else if (nt == 128) fused_launch<T, D, kLExact, 128>(L, pa, pb, nl, lbuf, lstride, ovf, st);
+  else fused_launch<T, D, kLExact, 64>(L, pa, pb, nl, lbuf, lstride, ovf, st);
+}
+
+template <typename T>
+void launch_line_fused(const LevelView<T>& L, int d, int color, void* lbuf, int lf, int nt,
+                       int* ovf, cudaStream_t st) {
+  if (d == 0) line_fused_d<T, 0>(L, color, lbuf, lf, nt, ovf, st);
+  else if (d == 1) line_fused_d<T, 1>(L, color, lbuf, lf, nt, ovf, st);
+  else line_fused_d<T, 2>(L, color, lbuf, lf, nt, ovf, st);
+}
+template void launch_line_fused<float>(const LevelView<float>&, int, int, void*, int, int, int*,
+                                       cudaStream_t);
+template void launch_line_fused<double>(const LevelView<double>&, int, int, void*, int, int, int*,
+                                        cudaStream_t);
+
 // ------------------------------------------------------------ point sweep
 // row (C, side): side 0 = E_C(N - e_C), side 1 = E_C(N); patch index 2C+side.
 template <typename T, int C, int SIDE>

@@ -60,6 +60,19 @@ template <typename T>
 void launch_line_sweep_fac(const LevelView<T>& L, int d, int color, const T* fac, const int* grp,
                            C_t<T>* rb, int fmt, cudaStream_t st, SweepShape sh = SweepShape());
 
+// one colour of line relaxation along d in one launch (k_line_fused): each
+// thread assembles, factors and solves one line; z waits in L.r (the
+// level's residual buffer, dead while the level smooths) at each row's slot
+// and the line's multipliers in lbuf, line_l_bytes per RHS: lf = kLExact
+// keeps them in T precision, kLHalf (T = float) in fp16 (both substitutions
+// use the rounded values; *ovf set when one leaves the fp16 range).  nt:
+// lines per block (32, 64 or 128; no value changes any thread's arithmetic)
+constexpr int kLExact = 0, kLHalf = 1;
+long line_l_bytes(const int n[3], int d, int color, int lf, int tsize);
+template <typename T>
+void launch_line_fused(const LevelView<T>& L, int d, int color, void* lbuf, int lf, int nt,
+                       int* ovf, cudaStream_t st);
+
 template <typename T>
 void launch_point_sweep(const LevelView<T>& L, int color, cudaStream_t st);
 

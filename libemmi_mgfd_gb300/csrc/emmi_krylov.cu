@@ -392,6 +392,14 @@ int krylov_solve(emmi_solver* s, std::vector<int>& cycles, std::vector<int>& sta
                        st));
     CK(cudaMemcpyAsync(nrm.data(), s->d_norm64, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    // an fp16 multiplier of the line sweep out of range: redo this
+    // preconditioner application with working-precision multipliers
+    if ((rc = line_format_fallback(s)) < 0) return rc;
+    if (rc == 1) {
+      rc = EMMI_OK;
+      app--;
+      continue;
+    }
     for (size_t q = 0; q < hh.size(); q++) {
       hh[q].x += hh2[q].x;
       hh[q].y += hh2[q].y;

@@ -175,13 +175,14 @@ __device__ __forceinline__ uint32_t mbar_test(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok;
 }
-// a wait that gives up after about a second (false): the caller records the
-// failure and leaves without touching the data
+// a wait that gives up after `limit` clocks (false; about a second by
+// default): the caller records the failure and leaves without touching the
+// data
 constexpr long long kWaitCycles = 2000000000LL;
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
   while (!mbar_test(bar, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
@@ -265,6 +266,9 @@ struct ConvArgs {
   int W;         // window slots: 128 + 2X + 3
   int wbytes;    // window stride in shared memory (16 W rounded up to 128)
   const int* mask;
+  long long wait;  // clocks a wait gives up after (kWaitCycles)
+  int stall;       // test hook: 1 = the producer issues no copy and no MMA, so
+                   // the epilogue's first wait has nothing to wait for
 };
 
 constexpr int kTcEpiWarps = 4;  // epilogue warps (TMEM lanes 0..127); one producer warp
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(kTcThreads) k_ls_conv(ConvArgs a, const uint4*
 
   if (warp == kTcEpiWarps) {
     // ---- producer: one thread issues the window copies and the MMAs
-    if ((tid & 31) == 0) {
+    if ((tid & 31) == 0 && !a.stall) {
       const uint4* inb = in + (long)b * a.S;
       int issued = k0 - 2, waited = k0 - 2, committed = k0 - 1;
       auto load = [&](int p) {
@@ -353,10 +357,10 @@ __global__ void __launch_bounds__(kTcThreads) k_ls_conv(ConvArgs a, const uint4*
         bool ok = true;
         // accumulator acc(k) and the window slot of plane k-3 are free once
         // the epilogue of plane k-2 has read its accumulator back
-        if (k - 2 >= k0) ok = mbar_wait(su32(&bar_free[acc(k)]), use(k) ^ 1u);
+        if (k - 2 >= k0) ok = mbar_wait(su32(&bar_free[acc(k)]), use(k) ^ 1u, a.wait);
         if (ok && k + kTcAhead <= k1) load(k + kTcAhead);
         for (int p = waited + 1; p <= k + 1 && ok; p++) {
-          ok = mbar_wait(su32(&bar_full[slot(p)]), parity(p));
+          ok = mbar_wait(su32(&bar_full[slot(p)]), parity(p), a.wait);
           if (ok) waited = p;
         }
         if (!ok || failed) {
@@ -383,8 +387,9 @@ __global__ void __launch_bounds__(kTcThreads) k_ls_conv(ConvArgs a, const uint4*
       }
       if (failed) {
         // copies and MMAs in flight finish before shared and tensor memory go
-        for (int p = waited + 1; p <= issued; p++) mbar_wait(su32(&bar_full[slot(p)]), parity(p));
-        if (committed >= k0) mbar_wait(su32(&bar_done[acc(committed)]), use(committed));
+        for (int p = waited + 1; p <= issued; p++)
+          mbar_wait(su32(&bar_full[slot(p)]), parity(p), a.wait);
+        if (committed >= k0) mbar_wait(su32(&bar_done[acc(committed)]), use(committed), a.wait);
       }
     }
   } else {
@@ -393,7 +398,7 @@ __global__ void __launch_bounds__(kTcThreads) k_ls_conv(ConvArgs a, const uint4*
     const bool live = p < a.XY;
     const int j = live ? p / a.X : 0, i = p - j * a.X;
     for (int k = k0; k < k1; k++) {
-      const bool late = !mbar_wait(su32(&bar_done[acc(k)]), use(k));
+      const bool late = !mbar_wait(su32(&bar_done[acc(k)]), use(k), a.wait);
       // the warp leaves together (tcgen05.ld below is warp-collective)
       if (__any_sync(0xffffffffu, late || failed)) {
         if (late) {
@@ -599,6 +604,8 @@ ConvArgs conv_args(const int n[3], const int* mask) {
   a.W = 128 + 2 * a.X + 3;
   a.wbytes = (16 * a.W + 127) / 128 * 128;
   a.mask = mask;
+  a.wait = kWaitCycles;
+  a.stall = 0;
   return a;
 }
 
@@ -635,12 +642,15 @@ void learned_pack(const float* dW32, uint4* dWt, cudaStream_t st) {
   k_ls_pack<<<(2 * kTcInstr * 32 + 127) / 128, 128, 0, st>>>(dW32, dWt);
 }
 
-// u += N(D^-1 (f - A u)) on the RHS that mask selects (level-0 view L)
+// u += N(D^-1 (f - A u)) on the RHS that mask selects (level-0 view L);
+// wait > 0 / stall: the convolutions' wait limit and test stall (ConvArgs)
 void learned_apply(const LevelView<float>& L, const uint4* Wt, uint32_t* X, uint32_t* H,
-                   cudaStream_t st) {
+                   cudaStream_t st, long long wait = 0, int stall = 0) {
   dim3 g1((unsigned)((L.S + 255) / 256), L.nrhs);
   k_ls_input<<<g1, 256, 0, st>>>(L, nullptr, X);
   ConvArgs a = conv_args(L.n, L.active);
+  if (wait > 0) a.wait = wait;
+  a.stall = stall;
   launch_conv<0>(a, L.nrhs, X, Wt, H, nullptr, st);
   launch_conv<1>(a, L.nrhs, H, Wt + kTcInstr * 32, nullptr, L.u, st);
 }
@@ -993,12 +1003,22 @@ int emmi_learned_apply(emmi_solver* s, const void* f, void* u) {
   L.f = reinterpret_cast<float2*>(const_cast<void*>(f));
   L.u = reinterpret_cast<float2*>(u);
   L.active = nullptr;
-  learned_apply(L, s->d_lsWt, s->d_lsX, s->d_lsH, s->st);
+  learned_apply(L, s->d_lsWt, s->d_lsX, s->d_lsH, s->st, s->ls_wait, s->ls_stall);
   LCK(cudaGetLastError());
   if (const int why = learned_check(s->st)) {
     set_err("emmi_learned_apply: a tensor-core convolution gave up waiting (code %d)", why);
     return EMMI_ECUDA;
   }
+  return EMMI_OK;
+}
+
+int emmi_learned_wait_hook(emmi_solver* s, long long wait_cycles, int stall) {
+  if (!s || wait_cycles < 0 || (stall != 0 && stall != 1)) {
+    set_err("emmi_learned_wait_hook: bad argument");
+    return EMMI_EINVAL;
+  }
+  s->ls_wait = wait_cycles;
+  s->ls_stall = stall;
   return EMMI_OK;
 }
 

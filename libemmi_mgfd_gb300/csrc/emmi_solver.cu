@@ -337,6 +337,11 @@ LevelView<float> emmi_solver::view<float>(int h, int l) const {
 template <typename T>
 static void line_colour(emmi_solver* s, int h, int l, int d, int col, const LevelView<T>& W,
                         int r0) {
+  if (s->opt.line_sweep) {
+    const int lf = std::is_same<T, float>::value ? s->lfmt : kLExact;
+    launch_line_fused<T>(W, d, col, s->scratch, lf, s->fused_nt[l][d], s->d_lovf, s->st);
+    return;
+  }
   if constexpr (std::is_same<T, float>::value) {
     if (s->fac_on) {
       const long off = s->fac_off[l == 0 ? 0 : h][l][d][col];
@@ -372,7 +377,7 @@ void emmi_solver::emit_smooth(int h, int l, int iter) {
           W.active += r0;
           W.op += r0;
           line_colour<T>(this, h, l, d, col, W, r0);
-          launch_counter += 3;  // assemble (residual), solve, apply
+          launch_counter += opt.line_sweep ? 1 : 3;  // fused, or residual / solve / apply
         }
       }
     }
@@ -804,6 +809,7 @@ void emmi_default_options(emmi_options* o) {
   o->krylov = 0;
   o->line_factors = 2;
   o->autotune = 1;
+  o->line_sweep = 0;
 }
 
 static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
@@ -1111,23 +1117,34 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
     // line-sweep scratch: largest (level, direction) over the hierarchies,
     // chunked over RHS so it stays below ~8 GB
     long per_rhs = 0;
+    const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
     for (int h = 0; h < 3; h++)
       for (int l = 0; l + 1 < s->lmax; l++)
         for (int d = 0; d < 3; d++)
-          if (s->hier[h][l + 1].sc[d] == 2)
+          if (s->hier[h][l + 1].sc[d] == 2) {
             per_rhs = std::max(per_rhs, line_scratch_elems(s->hier[h][l].n, d, 1));
-    const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+            // the one-launch sweep's multipliers (whole elements of esz)
+            for (int c = 0; c < 4; c++)
+              per_rhs = std::max<long>(
+                  per_rhs, (line_l_bytes(s->hier[h][l].n, d, c, kLExact, (int)esz / 2) + esz - 1) /
+                               (long)esz);
+          }
     const size_t cap = (size_t)8 << 30;
     s->chunk = s->nrhs;
     while (s->chunk > 1 && (size_t)per_rhs * esz * s->chunk > cap) s->chunk = (s->chunk + 1) / 2;
     s->scratch_bytes = std::max<size_t>((size_t)per_rhs * esz * s->chunk, 16);
     TRY(s->alloc(&s->scratch, s->scratch_bytes));
     if (mixed && s->opt.krylov > 0) TRY(krylov_alloc(s));
+    TRY(s->alloc((void**)&s->d_lovf, sizeof(int)));
+    CKS(cudaMemsetAsync(s->d_lovf, 0, sizeof(int), s->st));
+    s->lfmt = (mixed && s->opt.line_factors == 2) ? kLHalf : kLExact;
+    for (int l = 0; l < kMaxLev; l++)
+      for (int d = 0; d < 3; d++) s->fused_nt[l][d] = 64;
     mark("field buffers");
-    if (mixed && s->opt.line_factors) TRY(build_line_factors(s));
+    if (mixed && s->opt.line_factors && !s->opt.line_sweep) TRY(build_line_factors(s));
     mark("line factors");
-    if (mixed && s->opt.autotune > 0) TRY(autotune_sweeps(s));
-    if (mixed && s->opt.autotune < 0) {
+    if (mixed && s->opt.autotune > 0 && !s->opt.line_sweep) TRY(autotune_sweeps(s));
+    if (mixed && s->opt.autotune < 0 && !s->opt.line_sweep) {
       // a forced level-0 shape k = -autotune (1..10): substitution variant
       // (k-1) % 5, right-hand-side threads 256 for k <= 5, else 128
       const int k = std::min(-s->opt.autotune, 2 * kSubstVariants) - 1;
@@ -1157,6 +1174,28 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
 }
 
 }  // extern "C"
+
+int line_format_fallback(emmi_solver* s) {
+  if (!s->opt.line_sweep || s->lfmt != kLHalf) return 0;
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, s->d_lovf, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (!flag) return 0;
+  s->lfmt = kLExact;
+  CK(cudaMemsetAsync(s->d_lovf, 0, sizeof(int), s->st));
+  if (s->opt.use_graphs) {
+    CK(cudaStreamSynchronize(s->st));
+    for (int h = 0; h < 3; h++) {
+      if (s->gA[h]) cudaGraphExecDestroy(s->gA[h]);
+      if (s->gB[h]) cudaGraphExecDestroy(s->gB[h]);
+      s->gA[h] = s->gB[h] = nullptr;
+    }
+    const int rc = s->build_graphs<float>();
+    if (rc != EMMI_OK) return rc;
+  }
+  if (s->opt.verb) printf("line sweep: an fp16 multiplier left its range; fp32 from here on\n");
+  return 1;
+}
 
 int run_part(emmi_solver* s, int h, int part) {
   if (s->opt.use_graphs) {
@@ -1263,69 +1302,83 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
       if ((rc = run_part(s, hh, 0)) != EMMI_OK) return rc;
       if (s->has_norm) {
         if ((rc = read_norms(s, s->d_norm, nrm)) != EMMI_OK) return rc;
-        // complex64 estimate of |b - A(x+u)|; refine when it says converged
-        // or every refine_every cycles
-        bool anyref = false;
-        for (int r = 0; r < nrhs; r++) {
-          ref[r] = 0;
-          if (!act[r]) continue;
-          const double est = std::sqrt(nrm[r]) / rnorm0[r];
-          if (s->opt.verb) printf("icycle=%d rnorm=%e\n", icycle, est * rnorm0[r]);
-          if ((est < tol && since[r] > 0) || since[r] >= s->opt.refine_every || !std::isfinite(est)) {
-            ref[r] = 1;
-            anyref = true;
-          }
-        }
-        if (anyref) {
-          if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
+        if ((rc = line_format_fallback(s)) < 0) return rc;
+        if (rc == 1) {
+          // the last cycles' corrections carry the out-of-range multipliers:
+          // every cycling RHS restarts its inner problem from u = 0, whose
+          // level-0 residual (what part B restricts) is f
           dim3 g(blocks_for(n3s, 256, 2048), nrhs);
-          k_accumulate<<<g, 256, 0, s->st>>>(s->u64[0], s->u32[0], n3s, s->d_refine);
-          LevelView<double> W = s->view<double>(0, 0);
-          W.u = s->u64[0];
-          W.f = s->f64[0];
-          W.active = s->d_refine;
-          CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
-          true_residual64<float>(s, W, s->f32[0], s->d_norm64);
-          k_zero_masked<<<g, 256, 0, s->st>>>(s->u32[0], n3s, s->d_refine);
-          s->last_launches += 3;
-          if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
+          k_zero_masked<<<g, 256, 0, s->st>>>(s->u32[0], n3s, s->d_active);
+          LevelView<float> R = s->view<float>(hh, 0);
+          launch_residual<float, float>(R, R.r, nullptr, s->st);
+          s->last_launches += 2;
+          for (int r = 0; r < nrhs; r++) since[r] = 0;
+          rc = EMMI_OK;
+        } else {
+          // complex64 estimate of |b - A(x+u)|; refine when it says converged
+          // or every refine_every cycles
+          bool anyref = false;
           for (int r = 0; r < nrhs; r++) {
-            if (!ref[r]) continue;
-            nref[r]++;
-            since[r] = 0;
-            rn[r] = std::sqrt(nrm[r]);
-            const double rel = rn[r] / rnorm0[r];
-            const double prev_rel = last_rel[r];
-            last_rel[r] = rel;
-            if (!std::isfinite(rel)) {
-              act[r] = 0;
-              status[r] = EMMI_SOLVE_NONFINITE;
-            } else if (rel <= tol) {
-              act[r] = 0;
-              status[r] = EMMI_SOLVE_OK;
-            } else if (rel > 0.5 * prev_rel && learned_fallback(s, r)) {
-              // no halving since the last refinement with the learned
-              // correction on: continue with plain cycles
-              stall[r] = 0;
-            } else {
-              if (rel < 0.5 * best[r]) {
-                best[r] = rel;
-                stall[r] = 0;
-              } else if (++stall[r] >= 4) {
-                act[r] = 0;
-                status[r] = EMMI_SOLVE_STALL;
-              }
+            ref[r] = 0;
+            if (!act[r]) continue;
+            const double est = std::sqrt(nrm[r]) / rnorm0[r];
+            if (s->opt.verb) printf("icycle=%d rnorm=%e\n", icycle, est * rnorm0[r]);
+            if ((est < tol && since[r] > 0) || since[r] >= s->opt.refine_every || !std::isfinite(est)) {
+              ref[r] = 1;
+              anyref = true;
             }
           }
-          if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
-          // the new inner problem starts from u = 0: its level-0 residual
-          // (what part B restricts) is f; recompute it for the refined RHS
-          for (int r = 0; r < nrhs; r++) ref[r] = ref[r] && act[r];
-          if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
-          LevelView<float> R = s->view<float>(hh, 0);
-          R.active = s->d_refine;
-          launch_residual<float, float>(R, R.r, nullptr, s->st);
-          s->last_launches++;
+          if (anyref) {
+            if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
+            dim3 g(blocks_for(n3s, 256, 2048), nrhs);
+            k_accumulate<<<g, 256, 0, s->st>>>(s->u64[0], s->u32[0], n3s, s->d_refine);
+            LevelView<double> W = s->view<double>(0, 0);
+            W.u = s->u64[0];
+            W.f = s->f64[0];
+            W.active = s->d_refine;
+            CK(cudaMemsetAsync(s->d_norm64, 0, nrhs * sizeof(double), s->st));
+            true_residual64<float>(s, W, s->f32[0], s->d_norm64);
+            k_zero_masked<<<g, 256, 0, s->st>>>(s->u32[0], n3s, s->d_refine);
+            s->last_launches += 3;
+            if ((rc = read_norms(s, s->d_norm64, nrm)) != EMMI_OK) return rc;
+            for (int r = 0; r < nrhs; r++) {
+              if (!ref[r]) continue;
+              nref[r]++;
+              since[r] = 0;
+              rn[r] = std::sqrt(nrm[r]);
+              const double rel = rn[r] / rnorm0[r];
+              const double prev_rel = last_rel[r];
+              last_rel[r] = rel;
+              if (!std::isfinite(rel)) {
+                act[r] = 0;
+                status[r] = EMMI_SOLVE_NONFINITE;
+              } else if (rel <= tol) {
+                act[r] = 0;
+                status[r] = EMMI_SOLVE_OK;
+              } else if (rel > 0.5 * prev_rel && learned_fallback(s, r)) {
+                // no halving since the last refinement with the learned
+                // correction on: continue with plain cycles
+                stall[r] = 0;
+              } else {
+                if (rel < 0.5 * best[r]) {
+                  best[r] = rel;
+                  stall[r] = 0;
+                } else if (++stall[r] >= 4) {
+                  act[r] = 0;
+                  status[r] = EMMI_SOLVE_STALL;
+                }
+              }
+            }
+            if ((rc = upload_mask(s, s->d_active, act)) != EMMI_OK) return rc;
+            // the new inner problem starts from u = 0: its level-0 residual
+            // (what part B restricts) is f; recompute it for the refined RHS
+            for (int r = 0; r < nrhs; r++) ref[r] = ref[r] && act[r];
+            if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
+            LevelView<float> R = s->view<float>(hh, 0);
+            R.active = s->d_refine;
+            launch_residual<float, float>(R, R.r, nullptr, s->st);
+            s->last_launches++;
+          }
         }
       }
       if ((rc = run_part(s, hh, 1)) != EMMI_OK) return rc;
@@ -1540,7 +1593,7 @@ int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int
   cudaEventElapsedTime(&t, s->ev0, s->ev1);
   const double c = mixed ? 8.0 : 16.0;
   if (ms) *ms = t / reps;
-  if (launches) *launches = 12 * ((s->nrhs + s->chunk - 1) / s->chunk);
+  if (launches) *launches = (s->opt.line_sweep ? 4 : 12) * ((s->nrhs + s->chunk - 1) / s->chunk);
   if (bytes) *bytes = (double)s->hier[0][0].S * (9 * c + 12) * s->nrhs;
   return EMMI_OK;
 }
@@ -1550,6 +1603,9 @@ long emmi_solver_last_launches(const emmi_solver* s) { return s ? s->last_launch
 size_t emmi_solver_device_bytes(const emmi_solver* s) { return s ? s->bytes : 0; }
 int emmi_solver_line_factor_format(const emmi_solver* s) {
   return s && s->fac_on ? s->fac_fmt : -1;
+}
+int emmi_solver_line_format(const emmi_solver* s) {
+  return s && s->opt.line_sweep ? s->lfmt : -1;
 }
 
 void emmi_solver_destroy(emmi_solver* s) {

@@ -95,6 +95,13 @@ struct emmi_solver {
   size_t fac_bytes = 0;
   long fac_off[3][emmi::kMaxLev][3][4];
 
+  // one-launch line sweep (opt.line_sweep): multiplier format (kLHalf only
+  // for MIXED with line_factors = 2), the device flag an fp16 multiplier out
+  // of range sets, and lines per block per (level, direction)
+  int lfmt = 0;
+  int* d_lovf = nullptr;
+  int fused_nt[emmi::kMaxLev][3];
+
   // stored FP64 edge coefficients of the level-0 true operators (MIXED):
   // the refinement residual reads them instead of recomputing (null: off)
   double* d_coef64 = nullptr;
@@ -117,6 +124,9 @@ struct emmi_solver {
   // [nrhs][S][8] between zero guards, per-RHS enable mask (cleared for a RHS
   // that falls back to plain cycles)
   bool learned_on = false;
+  // emmi_learned_apply's wait limit (clocks, 0 = default) and test stall
+  long long ls_wait = 0;
+  int ls_stall = 0;
   float* d_lsW = nullptr;
   uint4* d_lsWt = nullptr;
   uint32_t *d_lsX = nullptr, *d_lsH = nullptr;
@@ -144,6 +154,12 @@ struct emmi_solver {
 
 // one part of a cycle on hierarchy h (graph launch or direct emission)
 int run_part(emmi_solver* s, int h, int part);
+// the one-launch line sweep with fp16 multipliers saw one out of range
+// (reads the device flag; synchronizes the solver's stream): from then on
+// it keeps working-precision multipliers and the cycle graphs are
+// recaptured.  Returns 1 when it switched, 0 when nothing happened, <0 on a
+// CUDA error
+int line_format_fallback(emmi_solver* s);
 
 // FP64 r = f - A u on level 0 with the true operator (V a level-0 FP64
 // view): from the stored coefficients when the solver keeps them

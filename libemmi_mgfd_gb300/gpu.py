@@ -51,7 +51,7 @@ class _Options(C.Structure):
                 ("tol", C.c_double), ("isemicoarsen", C.c_int), ("precision", C.c_int),
                 ("sigma_floor", C.c_double), ("refine_every", C.c_int),
                 ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int),
-                ("line_factors", C.c_int), ("autotune", C.c_int)]
+                ("line_factors", C.c_int), ("autotune", C.c_int), ("line_sweep", C.c_int)]
 
 
 class _Stats(C.Structure):
@@ -107,11 +107,13 @@ class Options:
     krylov: int = 0
     line_factors: int = 2
     autotune: int = 1
+    line_sweep: int = 0
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
                         self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
-                        self.verb, self.krylov, self.line_factors, self.autotune)
+                        self.verb, self.krylov, self.line_factors, self.autotune,
+                        self.line_sweep)
 
 
 class Solver:
@@ -328,6 +330,12 @@ class Solver:
     def line_factor_format(self) -> int:
         """1: stored factors with L in fp16; 0: fp32; -1: none."""
         return lib().emmi_solver_line_factor_format(self._h)
+
+    @property
+    def line_format(self) -> int:
+        """Multipliers of the one-launch line sweep: 1 fp16, 0 working
+        precision, -1 the three-launch sweep."""
+        return lib().emmi_solver_line_format(self._h)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -19,6 +19,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 typedef double complex zc;
 
@@ -680,11 +681,27 @@ static void w_cycle(mg_t *M, lev_t *H, int l) {
   for (int i = 0; i < M->prm.v2; i++) smooth(M, H, l, i);
 }
 
+static double wall_seconds(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
 int eo_gmg_solve(int n1, int n2, int n3, const float *x1, const float *x2,
                  const float *x3, const float *sigma11, const float *sigma22,
                  const float *sigma33, const float *invmur, double omega,
                  const eo_params *prm, double *b, double *x,
                  double *rnorm_hist) {
+  return eo_gmg_solve_timed(n1, n2, n3, x1, x2, x3, sigma11, sigma22, sigma33, invmur, omega,
+                            prm, b, x, rnorm_hist, NULL);
+}
+
+int eo_gmg_solve_timed(int n1, int n2, int n3, const float *x1, const float *x2,
+                       const float *x3, const float *sigma11, const float *sigma22,
+                       const float *sigma33, const float *invmur, double omega,
+                       const eo_params *prm, double *b, double *x,
+                       double *rnorm_hist, double *seconds) {
+  const double t0 = wall_seconds();
   mg_t M;
   memset(&M, 0, sizeof(M));
   M.prm = *prm;
@@ -734,6 +751,7 @@ int eo_gmg_solve(int n1, int n2, int n3, const float *x1, const float *x2,
   M.lev = &L0;
 
   int ncycles = prm->ncycle;
+  const double t1 = wall_seconds();
   for (M.icycle = 0; M.icycle < prm->ncycle; M.icycle++) {
     int h = M.icycle % 3;
     if (!M.hier[h]) M.hier[h] = build_hierarchy(&M, h);
@@ -747,6 +765,10 @@ int eo_gmg_solve(int n1, int n2, int n3, const float *x1, const float *x2,
       ncycles = M.icycle;
       break;
     }
+  }
+  if (seconds) {
+    seconds[0] = t1 - t0;
+    seconds[1] = wall_seconds() - t1;
   }
   memcpy(x, L0.u, 3 * S * sizeof(zc));
   curl_h_lev(&L0, M.iwmu, L0.u, bz);

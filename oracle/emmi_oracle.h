@@ -50,6 +50,15 @@ int eo_gmg_solve(int n1, int n2, int n3,
                  const float *sigma33, const float *invmur,
                  double omega, const eo_params *prm,
                  double *b, double *x, double *rnorm_hist);
+/* The same with wall-clock timing: seconds[0] = set-up before the first
+ * cycle (level-0 arrays, volume scaling), seconds[1] = the cycles (each
+ * hierarchy built at its first use inside them). */
+int eo_gmg_solve_timed(int n1, int n2, int n3,
+                       const float *x1, const float *x2, const float *x3,
+                       const float *sigma11, const float *sigma22,
+                       const float *sigma33, const float *invmur,
+                       double omega, const eo_params *prm,
+                       double *b, double *x, double *rnorm_hist, double *seconds);
 
 /* ---- single-level operators, for kernel parity ------------------------- */
 /* A level is described by double node coordinates x[d] (n_d+1 values) and

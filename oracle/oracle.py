@@ -55,6 +55,7 @@ def lib():
         build()
         _lib = C.CDLL(LIB_PATH)
         _lib.eo_gmg_solve.restype = C.c_int
+        _lib.eo_gmg_solve_timed.restype = C.c_int
         _lib.eo_find_index.restype = C.c_int
     return _lib
 
@@ -77,17 +78,21 @@ def _c128(a) -> np.ndarray:
 
 def gmg_solve(n, x1, x2, x3, sigma11, sigma22, sigma33, invmur, omega, b,
               cycleopt=2, ncycle=30, v1=1, v2=1, tol=1e-6, isemicoarsen=1,
-              ordering=ORDER_LEX, verb=0):
-    """Reference-algorithm solve (gmg_apply).  Returns (E, H, ncycles, rnorms)."""
+              ordering=ORDER_LEX, verb=0, timing=False):
+    """Reference-algorithm solve (gmg_apply).  Returns (E, H, ncycles, rnorms),
+    and with timing=True also (set-up seconds, seconds of the cycles)."""
     prm = _Params(cycleopt, ncycle, v1, v2, tol, isemicoarsen, ordering, verb)
     bb = _c128(b).copy()
     x = np.zeros_like(bb)
     hist = np.full(ncycle + 1, np.nan)
+    sec = np.zeros(2)
     keep = [_f32(x1), _f32(x2), _f32(x3), _f32(sigma11), _f32(sigma22), _f32(sigma33),
             _f32(invmur)]
-    nc = lib().eo_gmg_solve(int(n[0]), int(n[1]), int(n[2]), *[_p(k) for k in keep],
-                            C.c_double(float(np.float32(omega))), C.byref(prm), _p(bb), _p(x),
-                            _p(hist))
+    nc = lib().eo_gmg_solve_timed(int(n[0]), int(n[1]), int(n[2]), *[_p(k) for k in keep],
+                                  C.c_double(float(np.float32(omega))), C.byref(prm), _p(bb),
+                                  _p(x), _p(hist), _p(sec))
+    if timing:
+        return x, bb, nc, hist[: nc + 1], (float(sec[0]), float(sec[1]))
     return x, bb, nc, hist[: nc + 1]
 
 

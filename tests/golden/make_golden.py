@@ -231,6 +231,9 @@ def _receivers_one(s: W.Survey, shot: int, extra):
            "x1": load(d, "x1", f32), "x2": load(d, "x2", f32), "x3": load(d, "x3", f32),
            "cycles": np.array([len(h) - 1 for h in hist], np.int32),
            "rnorm_last": np.array([h[-1] / h[0] if h else np.nan for h in hist], np.float64)}
+    # the printed residual history of each frequency's solve (gmg.c:1627)
+    for f, h in enumerate(hist):
+        out[f"rnorm_f{f}"] = np.array(h, np.float64)
     subprocess.run(["rm", "-rf", d])
     return out
 

@@ -118,3 +118,40 @@ def test_trained_network_gain_on_held_out_models():
     assert all(q["status"] == "ok" and q["rel"] <= 1e-8 for q in plain + learned)
     assert sum(c1) <= sum(c0)
     assert not any(q["fallback"] for q in learned)
+
+
+@gpu
+def test_convolution_wait_that_runs_out_reports_and_recovers(golden):
+    """The tensor-core convolution's bounded waits: with the test hook the
+    producer issues no copy and no MMA, so the epilogue waits on an
+    accumulator nothing will fill; with a limit of 2e6 clocks (about a
+    millisecond) the wait runs out, the kernel frees its tensor memory and
+    returns, emmi_learned_apply reports the failure, and on the same GPU
+    the next application and a full solve succeed."""
+    import ctypes as C
+    import torch
+    from libemmi_mgfd_gb300 import gpu as G
+    g = golden("tiny_layered")
+    n, x, raw, om = golden_level(g)
+    s = G.Solver(n, *[v.astype(np.float32) for v in x], raw[None], np.array([om], np.float32),
+                 options=G.Options(precision=G.PREC_MIXED, ncycle=60, tol=1e-8))
+    rng = np.random.default_rng(9)
+    W = 0.05 * rng.standard_normal((2, TAPS, CH, CH))
+    W[0, :, 6:, :] = 0.0
+    s.set_learned(W.astype(np.float32).reshape(-1))
+    shape = (1, 3 * s.nslots)
+    f = torch.complex(torch.randn(shape, device="cuda"), torch.randn(shape, device="cuda"))
+    u = torch.zeros_like(f)
+    L = G.lib()
+    L.emmi_learned_wait_hook.argtypes = [C.c_void_p, C.c_longlong, C.c_int]
+    L.emmi_learned_wait_hook.restype = C.c_int
+    assert L.emmi_learned_wait_hook(s._h, 2000000, 1) == 0
+    with pytest.raises(RuntimeError, match="gave up waiting"):
+        s.learned_apply(f, u)
+    assert torch.count_nonzero(u).item() == 0  # nothing written
+    assert L.emmi_learned_wait_hook(s._h, 0, 0) == 0
+    s.learned_apply(f, u)
+    assert torch.isfinite(torch.view_as_real(u)).all() and torch.count_nonzero(u).item() > 0
+    xs, hs, st = s.solve(g["b_f0"][None])
+    assert st[0]["status"] == "ok", st
+    s.close()

@@ -206,7 +206,7 @@ def test_stored_line_factors_give_the_same_iterates(golden):
         s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
                      op=np.zeros(3, np.int32),
                      options=G.Options(precision=G.PREC_MIXED, ncycle=6, tol=0.0,
-                                       sigma_floor=2e-4, line_factors=lf))
+                                       sigma_floor=2e-4, line_factors=lf, line_sweep=0))
         x, h, st = s.solve(bs)
         out[lf] = (x, h, [q["cycles"] for q in st], s.device_bytes)
         s.close()
@@ -234,7 +234,7 @@ def test_fp16_line_factors_converge_like_fp32(golden):
         s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
                      op=np.zeros(3, np.int32),
                      options=G.Options(precision=G.PREC_MIXED, ncycle=120, tol=1e-8,
-                                       sigma_floor=2e-4, line_factors=lf))
+                                       sigma_floor=2e-4, line_factors=lf, line_sweep=0))
         x, h, st = s.solve(bs)
         out[lf] = (x, h, st)
         s.close()
@@ -266,7 +266,7 @@ def test_fp16_factor_overflow_falls_back_to_fp32():
         x = [np.arange(9, dtype=np.float32) * dx, np.arange(9, dtype=np.float32) * 100.0,
              np.arange(9, dtype=np.float32) * 100.0]
         s = G.Solver(n, *x, raw[None], np.array([6.28], np.float32),
-                     options=G.Options(precision=G.PREC_MIXED, ncycle=3, tol=0.0))
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=3, tol=0.0, line_sweep=0))
         fmts[name] = s.line_factor_format
         xs, hs, st = s.solve(b)
         assert np.all(np.isfinite(xs)), name
@@ -306,7 +306,7 @@ def test_sweep_shapes_never_change_the_result(golden):
         s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
                      op=np.zeros(3, np.int32),
                      options=G.Options(precision=G.PREC_MIXED, ncycle=6, tol=0.0,
-                                       sigma_floor=2e-4, autotune=autotune))
+                                       sigma_floor=2e-4, autotune=autotune, line_sweep=0))
         x, h, st = s.solve(bs)
         shapes = s.sweep_shapes()
         s.close()
@@ -338,7 +338,7 @@ raw = np.concatenate([10.0 ** rng.uniform(-2, 0, (3,) + n[::-1]),
                       np.ones((1,) + n[::-1])]).astype(np.float32)
 x = [np.arange(v + 1, dtype=np.float32) * 100.0 for v in n]
 s = G.Solver(n, *x, raw[None], np.full(2, 6.28, np.float32), op=np.zeros(2, np.int32),
-             options=G.Options(precision=G.PREC_MIXED, ncycle=2, tol=0.0))
+             options=G.Options(precision=G.PREC_MIXED, ncycle=2, tol=0.0, line_sweep=0))
 print(json.dumps(s.sweep_shapes()))
 s.close()
 """
@@ -418,3 +418,67 @@ def test_config2_batch_mixed_matches_fp64_solve():
             worst = max(worst, float(np.abs(d[r, c] - d64[r, c]).max() / mx))
     print(f"largest receiver error vs FP64: {worst:.2e}")
     assert worst < 1e-4, worst
+
+
+@gpu
+@pytest.mark.parametrize("prec, lf", [(1, 2), (1, 1), (0, 2)])
+def test_one_launch_line_sweep_gives_the_three_launch_iterates(golden, prec, lf):
+    """The one-launch line sweep (default) against the three-launch sweep
+    with the same multiplier arithmetic -- stored fp16 L (lf 2) or fp32
+    (lf 1) for complex64 cycles, records for FP64 -- after six cycles of
+    three RHS: the same operations in the same order, so only the
+    compiler's multiply-add fusion differs (roundoff, amplified in the air
+    layer's curl-free E: compared below the sea surface and in H)."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"]])
+    oms = np.array([om, om, 0.5 * om], np.float32)
+    out = {}
+    for sweep in (1, 0):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
+                     op=np.zeros(3, np.int32),
+                     options=G.Options(precision=prec, ncycle=6, tol=0.0, sigma_floor=2e-4,
+                                       line_factors=lf, line_sweep=sweep))
+        x, h, st = s.solve(bs)
+        fmt = s.line_format
+        out[sweep] = (x, h, [q["cycles"] for q in st], s.last_launches)
+        s.close()
+        if sweep == 1:
+            assert fmt == (1 if (prec == 1 and lf == 2) else 0), fmt
+    assert out[1][2] == out[0][2] == [6, 6, 6]
+    assert out[1][3] < out[0][3]  # one launch per colour instead of three
+    sea = below_sea_mask(n, g["x3"])
+    tol = 1e-6 if prec == 1 else 1e-10
+    for r in range(3):
+        assert rel_err(out[1][0][r], out[0][0][r], sea) < tol
+        assert rel_err(out[1][1][r], out[0][1][r]) < tol
+
+
+@gpu
+def test_one_launch_sweep_fp16_overflow_switches_to_fp32():
+    """Cells 10^6 times thinner along x than along y and z: the x-line
+    multipliers leave the fp16 range during the first cycle; the solver
+    notices at the next norm check, keeps fp32 multipliers from then on and
+    restarts its inner cycles, so the solve stays finite and reduces its
+    residual (a normal grid keeps fp16)."""
+    G = _G()
+    n = (8, 8, 8)
+    rng = np.random.default_rng(3)
+    raw = np.concatenate([10.0 ** rng.uniform(-2, 0, (3, 8, 8, 8)),
+                          np.ones((1, 8, 8, 8))]).astype(np.float32)
+    b = np.zeros((1, 3 * 9 ** 3), np.complex128)
+    b[0, 3 * 9 ** 3 // 2] = 1.0
+    fmts = {}
+    for name, dx in (("normal", 100.0), ("thin", 1e-4)):
+        x = [np.arange(9, dtype=np.float32) * dx, np.arange(9, dtype=np.float32) * 100.0,
+             np.arange(9, dtype=np.float32) * 100.0]
+        s = G.Solver(n, *x, raw[None], np.array([6.28], np.float32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=12, tol=1e-6,
+                                       line_sweep=1))
+        xs, hs, st = s.solve(b)
+        fmts[name] = s.line_format
+        assert np.all(np.isfinite(xs)), name
+        assert st[0]["status"] != "nonfinite" and st[0]["rel"] < 0.5, (name, st)
+        s.close()
+    assert fmts == {"normal": 1, "thin": 0}, fmts

@@ -42,3 +42,31 @@ def test_ctypes_mirror_matches_the_c_struct(c_layout, cname):
     assert C.sizeof(py) == c_layout[(cname, "size")], cname
     for fname, _ in py._fields_:
         assert getattr(py, fname).offset == c_layout[(cname, fname)], (cname, fname)
+
+
+def _dropin_layout():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_ref_layout", os.path.join(ROOT, "tests", "golden", "make_ref_layout.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    members = mk.dropin_members(os.path.join(ROOT, "include", "emmi_dropin.h"))
+    src = mk.layout_program(members, "emmi_", ["emmi_dropin.h"])
+    return mk, mk.run_layout(src, os.path.join(ROOT, "include"))
+
+
+def test_dropin_structs_have_the_reference_layout():
+    """include/emmi_dropin.h against the reference's emf_t / acq_t / fwi_t
+    (include/emf.h:4-48, acq.h:4-19, fwi.h:4-28): every member's offset and
+    each struct's size, from the table tests/golden/make_ref_layout.py
+    compiled out of the reference's own headers; where those headers are
+    present (REF_ROOT, default: a checkout named `reference` beside this
+    repository) the table is also rebuilt from them live."""
+    import json
+    mk, ours = _dropin_layout()
+    with open(os.path.join(ROOT, "tests", "golden", "ref_struct_layout.json")) as f:
+        ref = json.load(f)["layout"]
+    assert ours == ref
+    ref_root = os.environ.get("REF_ROOT", os.path.join(os.path.dirname(ROOT), "reference"))
+    if os.path.exists(os.path.join(ref_root, "include", "emf.h")):
+        assert mk.reference_layout(ref_root) == ours
