@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-config5", action="store_true",
+                   help="skip the 256x256x128 learned-vs-plain configuration (config5)")
     p.add_argument("--no-parity", action="store_true",
                    help="skip the receiver parity report (FP64 solve of the batch to 1e-12)")
     p.add_argument("--no-fwi", action="store_true",
@@ -177,6 +179,71 @@ def fwi_eval_bench(n: int, tol: float):
     return out
 
 
+def config5_bench(a):
+    """The learned-smoother configuration: 50 shots of the log-normal model
+    family on a 256 x 256 x 128 mesh (about 25 M edge unknowns each), V(1,1)
+    cycles to 1e-8, with and without the learned correction.  The network is
+    trained on the GPU by the library's kernels on residuals of plain cycles
+    on random survey models (water over log-normal sediment with a resistive
+    body, through the host front end) at 96^3; the cells of the 50 shots are
+    homogenized on the device.  Each variant: one untimed batch, one timed
+    (CUDA events on the solver's stream)."""
+    import torch
+    from libemmi_mgfd_gb300 import gpu as G
+    from libemmi_mgfd_gb300 import host
+    from libemmi_mgfd_gb300 import learned as LS
+    from libemmi_mgfd_gb300 import workloads as W
+    s = W.config5()
+    m = host.Model.from_survey(s)
+    src = s.sources.astype(np.float32).copy()
+    padded = m.padded()
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        axes = list(ex.map(lambda p: m.axes(*padded[:3], float(p[0]), float(p[1]), float(p[2])),
+                           src))
+    nsh = len(src)
+    dcells = torch.empty((nsh, 4, int(np.prod(s.n))), dtype=torch.float32, device="cuda")
+    G.homogenize_batch(padded, axes, s.n, dcells.data_ptr())
+    X = [np.stack([ax[k] for ax in axes]) for k in ("x1", "x2", "x3")]
+    om = np.full(nsh, np.float32(2 * np.pi * s.freqs[0]), np.float32)
+    srcr = src.copy()
+    srcr[:, 3:] = np.deg2rad(srcr[:, 3:])
+    rec = s.receivers.astype(np.float32).copy()
+    rec[:, 3:] = np.deg2rad(rec[:, 3:])
+    tr = LS.train(n=96, models=16, per_rhs=4, steps=300, lr=3e-3, seed=500)
+    out = {"workload": "c5_lognormal_256x256x128_50shots_1Hz", "cycle": "V(1,1)",
+           "tol": a.tol, "rhs": nsh,
+           "training": {"models": 16, "mesh": "96^3", "samples": int(tr["samples"]),
+                        "collect_seconds": round(tr["collect_seconds"], 2),
+                        "train_seconds": round(tr["train_seconds"], 2),
+                        "loss_end": round(float(tr["loss"][-1]), 4)}}
+    for name, wts in (("plain", None), ("learned", tr["weights"])):
+        sv = G.Solver(s.n, *X, dcells.data_ptr(), om, op=np.arange(nsh, dtype=np.int32),
+                      options=G.Options(precision=G.PREC_MIXED, tol=a.tol, ncycle=100,
+                                        cycleopt=1),
+                      rho_water=np.float32(m.rho_water()))
+        if wts is not None:
+            sv.set_learned(wts)
+        sv.modelling(srcr, rec, s.chsrc, s.chrec)
+        ext = torch.cuda.ExternalStream(sv.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        _, st, _ = sv.modelling(srcr, rec, s.chsrc, s.chrec)
+        e1.record(ext)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        out[name] = {"seconds": round(t, 3), "solves_per_s": round(nsh / t, 3),
+                     "cycles_mean": float(np.mean([q["cycles"] for q in st])),
+                     "cycles_max": int(max(q["cycles"] for q in st)),
+                     "all_converged": all(q["status"] == "ok" for q in st),
+                     "max_rel_residual": float(max(q["rel"] for q in st)),
+                     "fallback_rate": float(np.mean([q["fallback"] for q in st]))}
+        sv.close()
+    del dcells
+    torch.cuda.empty_cache()
+    return out
+
+
 def parity_report(w, d, a):
     """Receiver errors of d (the benchmark's solve: [nrhs, nch, nrec]) against
     an FP64 solve of the same batch to 1e-12 and against the reference's
@@ -214,13 +281,14 @@ def parity_report(w, d, a):
     return out
 
 
-def make_solver(w, precision, tol, krylov=0, ncycle=100):
+def make_solver(w, precision, tol, krylov=0, ncycle=100, line_factors=2):
     from libemmi_mgfd_gb300 import gpu as G
     n = w["survey"].n
     nrhs = w["X1"].shape[0]
     return G.Solver(n, w["X1"], w["X2"], w["X3"], w["cells"], w["omega"],
                     op=np.arange(nrhs, dtype=np.int32),
-                    options=G.Options(precision=precision, tol=tol, ncycle=ncycle, krylov=krylov),
+                    options=G.Options(precision=precision, tol=tol, ncycle=ncycle, krylov=krylov,
+                                      line_factors=line_factors),
                     rho_water=w["rho_water"])
 
 
@@ -549,24 +617,33 @@ def main():
                "seconds_per_step": round(e2e_t, 4)}
 
     # plain FP64 GMG on the same batch
-    plain = None
+    # plain FP64 GMG (the reference's arithmetic) with its best line sweep
+    # (FP64 line factors stored at set-up), and with every line refactored in
+    # every sweep
+    plain, plain_rec = None, None
     if not a.no_fp64:
-        sp = make_solver(w, G.PREC_FP64, a.tol)
-        ext64 = torch.cuda.ExternalStream(sp.stream)
-        sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(ext64)
-        _, st64, _ = sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
-        e1.record(ext64)
-        e1.synchronize()
-        t64 = max_over_ranks(pg, e0.elapsed_time(e1) / 1e3)
-        ms64, _, by64 = sp.time_smoother(0, reps=2)
-        plain = {"value": round(nrhs * world / t64, 3), "unit": UNIT,
-                 "cycles_mean": float(np.mean([x["cycles"] for x in st64])),
-                 "all_converged": all(x["status"] == "ok" for x in st64),
-                 "smoother_GBps": round(by64 / (ms64 * 1e-3) / 1e9, 1)}
-        sp.close()
+        def fp64_arm(line_factors):
+            sp = make_solver(w, G.PREC_FP64, a.tol, line_factors=line_factors)
+            ext64 = torch.cuda.ExternalStream(sp.stream)
+            sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext64)
+            _, st64, _ = sp.modelling(w["src"], w["rec"], s.chsrc, s.chrec)
+            e1.record(ext64)
+            e1.synchronize()
+            t64 = max_over_ranks(pg, e0.elapsed_time(e1) / 1e3)
+            ms64, _, by64 = sp.time_smoother(0, reps=2)
+            out = {"value": round(nrhs * world / t64, 3), "unit": UNIT,
+                   "cycles_mean": float(np.mean([x["cycles"] for x in st64])),
+                   "all_converged": all(x["status"] == "ok" for x in st64),
+                   "smoother_GBps": round(by64 / (ms64 * 1e-3) / 1e9, 1),
+                   "line_factors": "stored FP64" if sp.line_factor_format == 0
+                                   else "refactored every sweep"}
+            sp.close()
+            return out
+        plain = fp64_arm(1)
+        plain_rec = fp64_arm(0)
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
@@ -579,6 +656,10 @@ def main():
     fwi = None
     if rank == 0 and world == 1 and not a.no_fwi:  # a one-GPU figure, like cpu_baseline
         fwi = fwi_eval_bench(a.n, a.tol)
+
+    c5 = None
+    if rank == 0 and world == 1 and not a.no_config5:
+        c5 = config5_bench(a)
 
     if rank == 0:
         line = {
@@ -603,8 +684,11 @@ def main():
             "learned": learned, "mixed_without_learned": without,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": round(value / plain["value"], 3) if plain else None,
+            "plain_fp64_refactoring": plain_rec,
+            "speedup_vs_plain_fp64_refactoring":
+                round(value / plain_rec["value"], 3) if plain_rec else None,
             "roofline": roof, "parity": parity, "cpu_baseline": cpu, "e2e": e2e,
-            "fwi_eval": fwi,
+            "fwi_eval": fwi, "config5": c5,
             "gpu_launches": timed_launches, "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

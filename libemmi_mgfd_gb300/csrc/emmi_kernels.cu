@@ -1301,6 +1301,11 @@ void init_line_kernels() {
     cudaFuncSetAttribute(k_line_factor<float, kFacF16>,
                          cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_factor<double, kFacF32>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_line_subst<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
   });
 }
 
@@ -2005,6 +2010,11 @@ template void launch_line_factor<float>(const LevelView<float>&, int, int, C_t<f
                                         int, int*, cudaStream_t);
 template void launch_line_sweep_fac<float>(const LevelView<float>&, int, int, const float*,
                                            const int*, C_t<float>*, int, cudaStream_t, SweepShape);
+template void launch_line_factor<double>(const LevelView<double>&, int, int, C_t<double>*,
+                                         double*, int, int*, cudaStream_t);
+template void launch_line_sweep_fac<double>(const LevelView<double>&, int, int, const double*,
+                                            const int*, C_t<double>*, int, cudaStream_t,
+                                            SweepShape);
 template void launch_residual<float, float>(const LevelView<float>&, C_t<float>*, double*, cudaStream_t);
 template void launch_residual<double, double>(const LevelView<double>&, C_t<double>*, double*, cudaStream_t);
 template void launch_residual<double, float>(const LevelView<double>&, C_t<float>*, double*, cudaStream_t);

@@ -342,14 +342,12 @@ static void line_colour(emmi_solver* s, int h, int l, int d, int col, const Leve
     launch_line_fused<T>(W, d, col, s->scratch, lf, s->fused_nt[l][d], s->d_lovf, s->st);
     return;
   }
-  if constexpr (std::is_same<T, float>::value) {
-    if (s->fac_on) {
-      const long off = s->fac_off[l == 0 ? 0 : h][l][d][col];
-      if (off >= 0) {
-        launch_line_sweep_fac<float>(W, d, col, s->d_fac + off, s->d_grp + r0,
-                                     (C_t<float>*)s->scratch, s->fac_fmt, s->st, s->shape[l][d]);
-        return;
-      }
+  if (s->fac_on) {
+    const long off = s->fac_off[l == 0 ? 0 : h][l][d][col];
+    if (off >= 0) {
+      launch_line_sweep_fac<T>(W, d, col, static_cast<const T*>(s->d_fac) + off, s->d_grp + r0,
+                               (C_t<T>*)s->scratch, s->fac_fmt, s->st, s->shape[l][d]);
+      return;
     }
   }
   launch_line_sweep<T>(W, d, col, (C_t<T>*)s->scratch, s->st);
@@ -491,12 +489,13 @@ int emmi_solver::build_graphs() {
 // colour) the smoother relaxes, and factor each group's lines once.  Leaves
 // fac_on false (factoring in every sweep) when they would take more than
 // half of the free device memory.
+template <typename T>
 static int build_line_factors(emmi_solver* s) {
   const int nrhs = s->nrhs;
   std::vector<int> grp(nrhs), gop;
-  std::vector<float> gw;
+  std::vector<T> gw;
   for (int r = 0; r < nrhs; r++) {
-    const float w = (float)((double)s->h_omega[r] * kMu0);
+    const T w = (T)((double)s->h_omega[r] * kMu0);
     int g = -1;
     for (int k = 0; k < (int)gop.size() && g < 0; k++)
       if (gop[k] == s->h_op[r] && gw[k] == w) g = k;
@@ -508,9 +507,10 @@ static int build_line_factors(emmi_solver* s) {
     grp[r] = g;
   }
   const int ng = (int)gop.size();
-  // fp16 L (the default, line_factors = 2) unless a value leaves its range;
-  // then every factor is recomputed in fp32
-  int fmt = s->opt.line_factors == 2 ? kFacF16 : kFacF32;
+  // complex64: fp16 L (the default, line_factors = 2) unless a value leaves
+  // its range, then every factor is recomputed in fp32; complex128: records
+  // in FP64
+  int fmt = (std::is_same<T, float>::value && s->opt.line_factors == 2) ? kFacF16 : kFacF32;
   int* d_ovf = nullptr;
   int rc;
   if ((rc = s->alloc((void**)&d_ovf, sizeof(int))) != EMMI_OK) return rc;
@@ -534,18 +534,17 @@ static int build_line_factors(emmi_solver* s) {
         }
     if (total == 0) return EMMI_OK;
     const size_t freeb = device_avail();
-    const size_t bytes = (size_t)total * sizeof(float);
+    const size_t bytes = (size_t)total * sizeof(T);
     if (bytes > freeb / 2) return EMMI_OK;  // factor in every sweep instead
     if ((rc = s->alloc((void**)&s->d_fac, bytes)) != EMMI_OK) return rc;
     if (!s->d_grp) {
       if ((rc = s->alloc((void**)&s->d_grp, nrhs * sizeof(int))) != EMMI_OK) return rc;
       if ((rc = s->alloc((void**)&s->d_gop, ng * sizeof(int))) != EMMI_OK) return rc;
-      if ((rc = s->alloc((void**)&s->d_gwmu, ng * sizeof(float))) != EMMI_OK) return rc;
+      if ((rc = s->alloc((void**)&s->d_gwmu, ng * sizeof(T))) != EMMI_OK) return rc;
       CK(cudaMemcpyAsync(s->d_grp, grp.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice,
                          s->st));
       CK(cudaMemcpyAsync(s->d_gop, gop.data(), ng * sizeof(int), cudaMemcpyHostToDevice, s->st));
-      CK(cudaMemcpyAsync(s->d_gwmu, gw.data(), ng * sizeof(float), cudaMemcpyHostToDevice,
-                         s->st));
+      CK(cudaMemcpyAsync(s->d_gwmu, gw.data(), ng * sizeof(T), cudaMemcpyHostToDevice, s->st));
     }
     CK(cudaMemsetAsync(d_ovf, 0, sizeof(int), s->st));
     s->ngroups = ng;
@@ -562,22 +561,23 @@ static int build_line_factors(emmi_solver* s) {
           const long off0 = s->fac_off[hb][l][d][0];
           if (std::find(done.begin(), done.end(), off0) != done.end()) continue;
           done.push_back(off0);
-          LevelView<float> V = s->view<float>(h, l);
+          LevelView<T> V = s->view<T>(h, l);
           V.op = s->d_gop;
-          V.wmu = s->d_gwmu;
+          V.wmu = static_cast<const T*>(s->d_gwmu);
           V.active = nullptr;
           for (int c = 0; c < 4; c++) {
             const long per = line_factor_elems(s->hier[h][l].n, d, c, fmt);
             for (int g0 = 0; g0 < ng; g0 += s->chunk) {
-              LevelView<float> W = V;
+              LevelView<T> W = V;
               W.nrhs = std::min(s->chunk, ng - g0);
               W.u += (long)g0 * 3 * V.S;
               W.f += (long)g0 * 3 * V.S;
               W.op += g0;
               W.wmu += g0;
-              launch_line_factor<float>(W, d, c, (C_t<float>*)s->scratch,
-                                        s->d_fac + s->fac_off[hb][l][d][c] + (long)g0 * per, fmt,
-                                        d_ovf, s->st);
+              launch_line_factor<T>(W, d, c, (C_t<T>*)s->scratch,
+                                    static_cast<T*>(s->d_fac) + s->fac_off[hb][l][d][c] +
+                                        (long)g0 * per,
+                                    fmt, d_ovf, s->st);
             }
           }
         }
@@ -1141,7 +1141,8 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
     for (int l = 0; l < kMaxLev; l++)
       for (int d = 0; d < 3; d++) s->fused_nt[l][d] = 64;
     mark("field buffers");
-    if (mixed && s->opt.line_factors && !s->opt.line_sweep) TRY(build_line_factors(s));
+    if (s->opt.line_factors && !s->opt.line_sweep)
+      TRY(mixed ? build_line_factors<float>(s) : build_line_factors<double>(s));
     mark("line factors");
     if (mixed && s->opt.autotune > 0 && !s->opt.line_sweep) TRY(autotune_sweeps(s));
     if (mixed && s->opt.autotune < 0 && !s->opt.line_sweep) {

@@ -81,17 +81,18 @@ struct emmi_solver {
 
   std::vector<int> h_active, h_refine;
 
-  // stored line factors (MIXED, opt.line_factors): RHS sharing an operator
-  // and a frequency form a group; d_fac holds the LDL^T factors of every
-  // line per group, in blocks per (hierarchy, level, direction, colour) at
-  // float offsets fac_off (-1: none; level 0 is shared by the hierarchies)
+  // stored line factors (opt.line_factors): RHS sharing an operator and a
+  // frequency form a group; d_fac holds the LDL^T factors of every line per
+  // group, in blocks per (hierarchy, level, direction, colour) at offsets
+  // fac_off in elements of the working precision (-1: none; level 0 is
+  // shared by the hierarchies)
   bool fac_on = false;
-  int fac_fmt = 0;          // 0: fp32 records; 1: fp16 L with fp32 1/d
+  int fac_fmt = 0;          // 0: records in working precision; 1: fp16 L with fp32 1/d
   int ngroups = 0;
   int* d_grp = nullptr;     // [nrhs] group of each RHS
   int* d_gop = nullptr;     // [ngroups] operator of each group
-  float* d_gwmu = nullptr;  // [ngroups] omega*mu0 of each group
-  float* d_fac = nullptr;
+  void* d_gwmu = nullptr;   // [ngroups] omega*mu0 of each group (working precision)
+  void* d_fac = nullptr;
   size_t fac_bytes = 0;
   long fac_off[3][emmi::kMaxLev][3][4];
 

@@ -227,6 +227,22 @@ def config3(n: int = 128, seed: int = 3) -> Survey:
                   rho.copy(), src, rec, all_pairs(len(sx), len(rxg)), [1.0], (n, n, n))
 
 
+def config5(n=(256, 256, 128), seed: int = 5) -> Survey:
+    """Learned-smoother configuration: the log-normal model family of
+    config3 (1000 m of water, log10 rho ~ N(0, 0.3) with 500 m correlation,
+    two resistive bodies of 20-100 ohm-m) under 50 shots on a 10 x 5 grid at
+    1 km, 1 Hz, 100 seafloor receivers, on a 256 x 256 x 128 mesh (about 25 M
+    edge unknowns per right-hand side)."""
+    s = config3(128, seed=seed)
+    sx, sy = np.meshgrid(np.arange(-4500.0, 4501.0, 1000.0), np.arange(-2000.0, 2001.0, 1000.0))
+    sx, sy = sx.ravel(), sy.ravel()
+    src = np.stack([sx, sy, np.full_like(sx, 950.0), np.zeros_like(sx), np.zeros_like(sx)],
+                   1).astype(np.float32)
+    return Survey("c5_lognormal", s.nx, s.ny, s.nz, s.dx, s.dy, s.dz, s.ox, s.oy, s.oz, s.rho11,
+                  s.rho22, s.rho33, src, s.receivers, all_pairs(len(sx), len(s.receivers)),
+                  [1.0], tuple(n))
+
+
 def config4(n: int = 128, seed: int = 4, true_model: bool = True) -> Survey:
     """Gradient mode: 25 shots x 3 frequencies (0.25, 0.5, 1 Hz), n^3 mesh.
     True model: a 100 ohm-m 4x4x0.1 km reservoir in 1 ohm-m sediment under

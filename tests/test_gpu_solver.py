@@ -482,3 +482,31 @@ def test_one_launch_sweep_fp16_overflow_switches_to_fp32():
         assert st[0]["status"] != "nonfinite" and st[0]["rel"] < 0.5, (name, st)
         s.close()
     assert fmts == {"normal": 1, "thin": 0}, fmts
+
+
+@gpu
+def test_fp64_stored_line_factors_give_the_same_iterates(golden):
+    """Complex128 cycles with the lines' LDL^T factors kept from set-up in
+    FP64 (line_factors = 1) against refactoring every line in every sweep
+    (line_factors = 0): the same operations in the same order, so the
+    iterates agree to roundoff after six cycles of three RHS."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"]])
+    oms = np.array([om, om, 0.5 * om], np.float32)
+    out = {}
+    for lf in (1, 0):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], oms,
+                     op=np.zeros(3, np.int32),
+                     options=G.Options(precision=G.PREC_FP64, ncycle=6, tol=0.0,
+                                       line_factors=lf))
+        x, h, st = s.solve(bs)
+        out[lf] = (x, h, [q["cycles"] for q in st], s.line_factor_format)
+        s.close()
+    assert out[1][3] == 0 and out[0][3] == -1
+    assert out[1][2] == out[0][2] == [6, 6, 6]
+    sea = below_sea_mask(n, g["x3"])
+    for r in range(3):
+        assert rel_err(out[1][0][r], out[0][0][r], sea) < 1e-10
+        assert rel_err(out[1][1][r], out[0][1][r]) < 1e-10
