@@ -91,6 +91,11 @@ typedef struct {
                        factors.  0 = three launches per colour (residual
                        rows, substitution, update) with the stored factors
                        of line_factors (default)                          */
+  int fused_level;  /* with line_sweep = 0: levels l >= fused_level use the
+                       one-launch sweep (their data sit in L2 and their
+                       launches are short); levels above it the three-launch
+                       sweep.  A value >= the number of levels keeps the
+                       three-launch sweep everywhere                      */
 } emmi_options;
 
 typedef struct {
@@ -125,7 +130,7 @@ int emmi_solver_solve(emmi_solver *s, const double *b, double *x, double *h,
 double emmi_solver_last_time(const emmi_solver *s);
 /* Multiplier format of the one-launch line sweep: 1 = fp16, 0 = working
  * precision (an fp16 multiplier out of range during a solve switches the
- * solver to 0 and restarts its inner cycles), -1 = the three-launch sweep. */
+ * solver to 0 and restarts its inner cycles), -1 = no level uses it. */
 int emmi_solver_line_format(const emmi_solver *s);
 /* Number of kernel launches in the last solve. */
 long emmi_solver_last_launches(const emmi_solver *s);

@@ -1066,16 +1066,36 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_subst(const int* __restr
 // pass LA and LB; the fp16 values are widened to fp32 and the arithmetic is
 // k_line_subst's.  NT lines per block, a cp.async ring of RING rows per
 // line: every thread's arithmetic is the same for every (NT, RING).
-template <int NT, int RING>
+//
+// D = 1 or 2 (y or z lines, whose neighbouring lines are neighbouring slots):
+// the backward pass also adds x to u at each row's slot (k_line_apply_rb's
+// work; the old u values ride the cp.async ring with the factors), so the
+// colour takes two launches and x never goes through the record buffer.
+// D = -1: x goes to rb for k_line_apply_rb.
+template <int D>
+__device__ __forceinline__ int subst_row_slot(const int n[3], long S, int ta, int tb, int row) {
+  const int s = row / 5 + 1, t = row - 5 * (s - 1);
+  switch (t) {
+    case 0: return (int)line_slot<D, 0>(n, S, ta, tb, s);
+    case 1: return (int)line_slot<D, 1>(n, S, ta, tb, s);
+    case 2: return (int)line_slot<D, 2>(n, S, ta, tb, s);
+    case 3: return (int)line_slot<D, 3>(n, S, ta, tb, s);
+    default: return (int)line_slot<D, 4>(n, S, ta, tb, s);
+  }
+}
+
+template <int NT, int RING, int D>
 __global__ void __launch_bounds__(NT) k_line_subst_h(const int* __restrict__ active,
                                                      const int* __restrict__ grp, long nl, int m,
                                                      long gstride, const float* __restrict__ fac,
-                                                     float2* __restrict__ rb) {
+                                                     float2* __restrict__ rb, LevelView<float> L,
+                                                     int pa, int pb, LineDiv dv) {
   constexpr int kRing = RING;
   __shared__ uint4 ra[kRing][NT];
   __shared__ uint32_t rl5[kRing][NT];
   __shared__ float2 rd[kRing][NT];
   __shared__ float2 rring[kRing][NT];
+  __shared__ float2 uring[D >= 1 ? kRing : 1][D >= 1 ? NT : 1];
   const int rhs = blockIdx.y;
   if (active && !active[rhs]) return;
   const int tid = threadIdx.x;
@@ -1083,6 +1103,15 @@ __global__ void __launch_bounds__(NT) k_line_subst_h(const int* __restrict__ act
   if (l >= nl) return;
   const HalfFac hf = half_fac(fac + (long)grp[rhs] * gstride, m, nl);
   float2* rr = rb + (long)rhs * m * nl + l;
+  float2* u = nullptr;
+  int ta = 0, tb = 0;
+  if constexpr (D >= 1) {
+    const LineGeom g = line_geom<D>(L.n, pa, pb);
+    const unsigned lq = fdiv((unsigned)l, dv.la);
+    ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la);
+    tb = g.fb + 2 * (int)lq;
+    u = L.u + (long)rhs * 3 * L.S;
+  }
   auto issue_l = [&](int row) {
     const int slot = row % kRing;
     cp_async16(&ra[slot][tid], hf.la + (long)row * nl + l);
@@ -1137,6 +1166,8 @@ __global__ void __launch_bounds__(NT) k_line_subst_h(const int* __restrict__ act
     if (q >= 0) {
       issue_l(q);
       cp_async8(&rring[q % kRing][tid], rr + (long)q * nl);
+      if constexpr (D >= 1)
+        cp_async8(&uring[q % kRing][tid], u + subst_row_slot<D>(L.n, L.S, ta, tb, q));
     }
     cp_async_commit();
   };
@@ -1152,7 +1183,10 @@ __global__ void __launch_bounds__(NT) k_line_subst_h(const int* __restrict__ act
 #pragma unroll
     for (int i = 4; i > 0; i--) xw[i] = xw[i - 1];
     xw[0] = x;
-    rr[(long)row * nl] = x;
+    if constexpr (D >= 1)
+      u[subst_row_slot<D>(L.n, L.S, ta, tb, row)] = cadd<float>(uring[row % kRing][tid], x);
+    else
+      rr[(long)row * nl] = x;
   }
   cp_async_wait<0>();
 }
@@ -1210,21 +1244,35 @@ constexpr int kSubstShape[kSubstVariants][2] = {{64, 6}, {32, 6}, {128, 6}, {64,
 int subst_variant_threads(int v) { return kSubstShape[v][0]; }
 int subst_variant_ring(int v) { return kSubstShape[v][1]; }
 
-template <int NT, int RING>
-static void subst_h_launch(long nl, int nrhs, const int* active, const int* grp, int m,
-                           long gstride, const float* fac, float2* rb, cudaStream_t st) {
-  dim3 g((unsigned)((nl + NT - 1) / NT), nrhs);
-  k_line_subst_h<NT, RING><<<g, NT, 0, st>>>(active, grp, nl, m, gstride, fac, rb);
+struct SubstArgs {
+  long nl;
+  int nrhs;
+  const int* active;
+  const int* grp;
+  int m;
+  long gstride;
+  const float* fac;
+  float2* rb;
+  LevelView<float> L;
+  int pa, pb;
+  LineDiv dv;
+};
+
+template <int NT, int RING, int D>
+static void subst_h_launch(const SubstArgs& a, cudaStream_t st) {
+  dim3 g((unsigned)((a.nl + NT - 1) / NT), a.nrhs);
+  k_line_subst_h<NT, RING, D><<<g, NT, 0, st>>>(a.active, a.grp, a.nl, a.m, a.gstride, a.fac,
+                                                a.rb, a.L, a.pa, a.pb, a.dv);
 }
 
-static void subst_h_variant(int v, long nl, int nrhs, const int* active, const int* grp, int m,
-                            long gstride, const float* fac, float2* rb, cudaStream_t st) {
+template <int D>
+static void subst_h_variant(int v, const SubstArgs& a, cudaStream_t st) {
   switch (v) {
-    case 1: subst_h_launch<32, 6>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
-    case 2: subst_h_launch<128, 6>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
-    case 3: subst_h_launch<64, 4>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
-    case 4: subst_h_launch<64, 8>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
-    default: subst_h_launch<64, 6>(nl, nrhs, active, grp, m, gstride, fac, rb, st); break;
+    case 1: subst_h_launch<32, 6, D>(a, st); break;
+    case 2: subst_h_launch<128, 6, D>(a, st); break;
+    case 3: subst_h_launch<64, 4, D>(a, st); break;
+    case 4: subst_h_launch<64, 8, D>(a, st); break;
+    default: subst_h_launch<64, 6, D>(a, st); break;
   }
 }
 
@@ -1242,16 +1290,22 @@ static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, con
   const LineDiv dv = line_div<D>(L.n, pa, pb);
   k_line_rhs<T, D><<<gr, rt, 0, st>>>(L, pa, pb, dv, rb);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
-  bool done = false;
   if constexpr (std::is_same<T, float>::value) {
     if (fmt == kFacF16) {
       const int v = sh.subst >= 0 && sh.subst < kSubstVariants ? sh.subst : 0;
-      subst_h_variant(v, nl, L.nrhs, L.active, grp, m, line_factor_elems(L.n, D, color, fmt), fac,
-                      rb, st);
-      done = true;
+      const SubstArgs a{nl, L.nrhs, L.active, grp, m, line_factor_elems(L.n, D, color, fmt),
+                        fac, rb, L, pa, pb, dv};
+      if constexpr (D == 0) {
+        subst_h_variant<-1>(v, a, st);
+      } else {
+        subst_h_variant<D>(v, a, st);  // the update rides the backward pass
+        return;
+      }
+      k_line_apply_rb<T, D><<<g1, 256, 0, st>>>(L, pa, pb, dv, rb);
+      return;
     }
   }
-  if (!done) k_line_subst<T><<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m, fac, rb);
+  k_line_subst<T><<<g2, kSolveThreads, 0, st>>>(L.active, grp, nl, m, fac, rb);
   k_line_apply_rb<T, D><<<g1, 256, 0, st>>>(L, pa, pb, dv, rb);
 }
 
@@ -1285,16 +1339,25 @@ void init_line_kernels() {
                          cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_line_subst<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_subst_h<64, 6>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_subst_h<32, 6>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_subst_h<128, 6>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_subst_h<64, 4>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_subst_h<64, 8>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
+    auto carve = [](const void* k) {
+      cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
+    };
+    carve((const void*)k_line_subst_h<64, 6, -1>);
+    carve((const void*)k_line_subst_h<32, 6, -1>);
+    carve((const void*)k_line_subst_h<128, 6, -1>);
+    carve((const void*)k_line_subst_h<64, 4, -1>);
+    carve((const void*)k_line_subst_h<64, 8, -1>);
+    carve((const void*)k_line_subst_h<64, 6, 1>);
+    carve((const void*)k_line_subst_h<32, 6, 1>);
+    carve((const void*)k_line_subst_h<128, 6, 1>);
+    carve((const void*)k_line_subst_h<64, 4, 1>);
+    carve((const void*)k_line_subst_h<64, 8, 1>);
+    carve((const void*)k_line_subst_h<64, 6, 2>);
+    carve((const void*)k_line_subst_h<32, 6, 2>);
+    carve((const void*)k_line_subst_h<128, 6, 2>);
+    carve((const void*)k_line_subst_h<64, 4, 2>);
+    carve((const void*)k_line_subst_h<64, 8, 2>);
     cudaFuncSetAttribute(k_line_factor<float, kFacF32>,
                          cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);

@@ -337,7 +337,7 @@ LevelView<float> emmi_solver::view<float>(int h, int l) const {
 template <typename T>
 static void line_colour(emmi_solver* s, int h, int l, int d, int col, const LevelView<T>& W,
                         int r0) {
-  if (s->opt.line_sweep) {
+  if (s->opt.line_sweep || l >= s->opt.fused_level) {
     const int lf = std::is_same<T, float>::value ? s->lfmt : kLExact;
     launch_line_fused<T>(W, d, col, s->scratch, lf, s->fused_nt[l][d], s->d_lovf, s->st);
     return;
@@ -351,6 +351,15 @@ static void line_colour(emmi_solver* s, int h, int l, int d, int col, const Leve
     }
   }
   launch_line_sweep<T>(W, d, col, (C_t<T>*)s->scratch, s->st);
+}
+
+// kernel launches of one colour of line relaxation along d on level l of
+// hierarchy h (what line_colour emits per RHS chunk)
+static int line_launches(const emmi_solver* s, int h, int l, int d) {
+  if (s->opt.line_sweep || l >= s->opt.fused_level) return 1;  // k_line_fused
+  if (s->fac_on && s->fac_off[l == 0 ? 0 : h][l][d][0] >= 0)
+    return (s->fac_fmt == kFacF16 && d != 0) ? 2 : 3;  // update in the substitution
+  return 3;
 }
 
 // smoothing (gmg.c:1301-1313): line relaxation along every direction the
@@ -375,7 +384,7 @@ void emmi_solver::emit_smooth(int h, int l, int iter) {
           W.active += r0;
           W.op += r0;
           line_colour<T>(this, h, l, d, col, W, r0);
-          launch_counter += opt.line_sweep ? 1 : 3;  // fused, or residual / solve / apply
+          launch_counter += line_launches(this, h, l, d);
         }
       }
     }
@@ -525,6 +534,7 @@ static int build_line_factors(emmi_solver* s) {
       for (int l = 0; l + 1 < s->lmax; l++)
         for (int d = 0; d < 3; d++) {
           if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
+          if (l >= s->opt.fused_level) continue;  // swept by the one-launch kernel
           const int hb = l == 0 ? 0 : h;
           if (s->fac_off[hb][l][d][0] >= 0) continue;
           for (int c = 0; c < 4; c++) {
@@ -557,6 +567,7 @@ static int build_line_factors(emmi_solver* s) {
       for (int l = 0; l + 1 < s->lmax; l++)
         for (int d = 0; d < 3; d++) {
           if (!s->opt.isemicoarsen || s->hier[h][l + 1].sc[d] != 2) continue;
+          if (l >= s->opt.fused_level) continue;  // swept by the one-launch kernel
           const int hb = l == 0 ? 0 : h;
           const long off0 = s->fac_off[hb][l][d][0];
           if (std::find(done.begin(), done.end(), off0) != done.end()) continue;
@@ -810,6 +821,7 @@ void emmi_default_options(emmi_options* o) {
   o->line_factors = 2;
   o->autotune = 1;
   o->line_sweep = 0;
+  o->fused_level = 99;
 }
 
 static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
@@ -1177,7 +1189,7 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
 }  // extern "C"
 
 int line_format_fallback(emmi_solver* s) {
-  if (!s->opt.line_sweep || s->lfmt != kLHalf) return 0;
+  if (!(s->opt.line_sweep || s->opt.fused_level < s->lmax) || s->lfmt != kLHalf) return 0;
   int flag = 0;
   CK(cudaMemcpyAsync(&flag, s->d_lovf, sizeof(int), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1594,7 +1606,7 @@ int emmi_solver_time_smoother(emmi_solver* s, int dir, int reps, double* ms, int
   cudaEventElapsedTime(&t, s->ev0, s->ev1);
   const double c = mixed ? 8.0 : 16.0;
   if (ms) *ms = t / reps;
-  if (launches) *launches = (s->opt.line_sweep ? 4 : 12) * ((s->nrhs + s->chunk - 1) / s->chunk);
+  if (launches) *launches = 4 * line_launches(s, h, 0, dir) * ((s->nrhs + s->chunk - 1) / s->chunk);
   if (bytes) *bytes = (double)s->hier[0][0].S * (9 * c + 12) * s->nrhs;
   return EMMI_OK;
 }
@@ -1606,7 +1618,7 @@ int emmi_solver_line_factor_format(const emmi_solver* s) {
   return s && s->fac_on ? s->fac_fmt : -1;
 }
 int emmi_solver_line_format(const emmi_solver* s) {
-  return s && s->opt.line_sweep ? s->lfmt : -1;
+  return s && (s->opt.line_sweep || s->opt.fused_level < s->lmax) ? s->lfmt : -1;
 }
 
 void emmi_solver_destroy(emmi_solver* s) {

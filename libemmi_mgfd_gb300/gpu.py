@@ -51,7 +51,8 @@ class _Options(C.Structure):
                 ("tol", C.c_double), ("isemicoarsen", C.c_int), ("precision", C.c_int),
                 ("sigma_floor", C.c_double), ("refine_every", C.c_int),
                 ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int),
-                ("line_factors", C.c_int), ("autotune", C.c_int), ("line_sweep", C.c_int)]
+                ("line_factors", C.c_int), ("autotune", C.c_int), ("line_sweep", C.c_int),
+                ("fused_level", C.c_int)]
 
 
 class _Stats(C.Structure):
@@ -108,12 +109,13 @@ class Options:
     line_factors: int = 2
     autotune: int = 1
     line_sweep: int = 0
+    fused_level: int = 99
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
                         self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
                         self.verb, self.krylov, self.line_factors, self.autotune,
-                        self.line_sweep)
+                        self.line_sweep, self.fused_level)
 
 
 class Solver:
