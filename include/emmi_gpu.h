@@ -132,6 +132,12 @@ double emmi_solver_last_time(const emmi_solver *s);
  * precision (an fp16 multiplier out of range during a solve switches the
  * solver to 0 and restarts its inner cycles), -1 = no level uses it. */
 int emmi_solver_line_format(const emmi_solver *s);
+/* 1 when every operator's invmur is exactly 1 (as the host front end
+ * writes it) and the complex64 operator therefore forms its coefficients
+ * from the mesh spacings (the cell weights being the cell volumes), 0 when
+ * it reads the volume-weighted invmur cells; the FP64 operator always reads
+ * them (the reference's arithmetic). */
+int emmi_solver_geometric_weights(const emmi_solver *s);
 /* Number of kernel launches in the last solve. */
 long emmi_solver_last_launches(const emmi_solver *s);
 /* Device bytes held by the solver. */

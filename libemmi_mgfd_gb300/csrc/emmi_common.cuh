@@ -90,6 +90,11 @@ template <typename T> struct LevelView {
   const int* active; // [nrhs] nonzero = work on this RHS (may be null)
   const int* op;     // [nrhs] operator (geo/cells) index of each RHS (null: identity)
   FastDiv d0, d1;    // division by n[0]+1 and n[1]+1 (set_slot_divs)
+  // nonzero: every cell's volume-weighted inverse permeability is its volume
+  // (the input invmur is exactly 1, as the front end writes it), so the
+  // coefficients come from the spacings alone (edge_coef); set only for the
+  // complex64 preconditioner operator
+  int imu_vol = 0;
 };
 
 // the slot-decode divisors of a view, set on the host wherever a view is built
@@ -171,10 +176,12 @@ __device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b
 __device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
 
 // P[3]: node indices of the edge; strides of the cell array; G geometry.
-template <typename T, int C>
+// W: the cell weights of the inverse permeability -- 0 read from the cells,
+// 1 the cell volumes (LevelView::imu_vol), 2 chosen by imu_vol at run time
+template <typename T, int C, int W = 2>
 __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const T* __restrict__ sigC,
                                           const T* __restrict__ imu, const Geo<T>& G, T wmu,
-                                          EdgeCoef<T>& e) {
+                                          EdgeCoef<T>& e, int imu_vol = 0) {
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
   const int a = P[C], b = P[p], g = P[q];
   // 32-bit cell offsets (a level has fewer than 2^31 cells)
@@ -184,18 +191,40 @@ __device__ __forceinline__ void edge_coef(const int n[3], const int P[3], const 
   const int c01 = c11 - cs[p];                         // (b-1, g)
   const int c00 = c01 - cs[q];                         // (b-1, g-1)
   const T s = T(0.25) * (((ldro(sigC + c00) + ldro(sigC + c01)) + ldro(sigC + c10)) + ldro(sigC + c11));
+  const T dc = ldro(G.ds(C) + a);
+  const T dpp = ldro(G.ds(p) + b), dpm = ldro(G.ds(p) + b - 1);
+  const T dqp = ldro(G.ds(q) + g), dqm = ldro(G.ds(q) + g - 1);
+  e.dim = -wmu * s;
+  if (W == 1 || (W == 2 && imu_vol)) {
+    // cell weight = volume: with the four cells' volumes dc*dp*dq the face
+    // averages give k_p+ = dc (dq+ + dq-) / (2 dp+) and so on, and the
+    // mixed terms reduce to (dq+ + dq-) / 2 and (dp+ + dp-) / 2
+    const T hq = T(0.5) * (dqp + dqm), hp = T(0.5) * (dpp + dpm);
+    const T kpp = qdiv(dc * hq, dpp), kpm = qdiv(dc * hq, dpm);
+    const T kqp = qdiv(dc * hp, dqp), kqm = qdiv(dc * hp, dqm);
+    e.dre = (kpp + kpm) + (kqp + kqm);
+    e.c[0] = -kpp;
+    e.c[1] = -kpm;
+    e.c[2] = -kqp;
+    e.c[3] = -kqm;
+    e.c[4] = hq;
+    e.c[5] = -hq;
+    e.c[6] = -hq;
+    e.c[7] = hq;
+    e.c[8] = hp;
+    e.c[9] = -hp;
+    e.c[10] = -hp;
+    e.c[11] = hp;
+    return;
+  }
   const T i00 = ldro(imu + c00), i01 = ldro(imu + c01), i10 = ldro(imu + c10), i11 = ldro(imu + c11);
   const T m1 = T(0.5) * (i11 + i10);  // H_q face at p=b
   const T m2 = T(0.5) * (i01 + i00);  // H_q face at p=b-1
   const T m3 = T(0.5) * (i11 + i01);  // H_p face at q=g
   const T m4 = T(0.5) * (i10 + i00);  // H_p face at q=g-1
-  const T dc = ldro(G.ds(C) + a);
-  const T dpp = ldro(G.ds(p) + b), dpm = ldro(G.ds(p) + b - 1);
-  const T dqp = ldro(G.ds(q) + g), dqm = ldro(G.ds(q) + g - 1);
   const T kpp = qdiv(m1, dpp * dpp), kpm = qdiv(m2, dpm * dpm);
   const T kqp = qdiv(m3, dqp * dqp), kqm = qdiv(m4, dqm * dqm);
   e.dre = (kpp + kpm) + (kqp + kqm);
-  e.dim = -wmu * s;
   e.c[0] = -kpp;
   e.c[1] = -kpm;
   e.c[2] = -kqp;
@@ -250,7 +279,8 @@ __device__ __forceinline__ void slot_nodes(long s, const LevelView<T>& L, int P[
 }
 
 // (A u) of the edge equation of component C at slot s, and its coefficients
-template <typename T, int C>
+// (W: edge_coef's cell weights)
+template <typename T, int C, int W = 2>
 __device__ __forceinline__ C_t<T> apply_row(const LevelView<T>& L, const C_t<T>* __restrict__ u,
                                             const T* __restrict__ cells, const Geo<T>& G, T wmu,
                                             const int P[3], long s, const long ss[3],
@@ -258,7 +288,7 @@ __device__ __forceinline__ C_t<T> apply_row(const LevelView<T>& L, const C_t<T>*
   // u, cells and geometry are not written by any thread while a residual,
   // an assembly or a same-colour block sweep reads them: read-only loads.
   // Offsets within the RHS's field are 32-bit.
-  edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
+  edge_coef<T, C, W>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e, L.imu_vol);
   const int si = (int)s, Si = (int)L.S;
   const int s3[3] = {1, (int)ss[1], (int)ss[2]};
   const C_t<T> uc = ldro(u + (C * Si + si));

@@ -137,7 +137,7 @@ __device__ __forceinline__ bool is_unknown(const int n[3], const int P[3]) {
   return P[C] < n[C] && P[p] >= 1 && P[p] < n[p] && P[q] >= 1 && P[q] < n[q];
 }
 
-template <typename T, typename TO, int C>
+template <typename T, typename TO, int C, int W>
 __device__ __forceinline__ T residual_comp(const LevelView<T>& L, const C_t<T>* u,
                                                 const C_t<T>* f, const T* cells, const Geo<T>& G,
                                                 T wmu, const int P[3], long s, const long ss[3],
@@ -146,7 +146,7 @@ __device__ __forceinline__ T residual_comp(const LevelView<T>& L, const C_t<T>* 
   C_t<T> r = f ? f[o] : mk<T>(0, 0);     // f null: r = -A u
   if (is_unknown<C>(L.n, P)) {
     EdgeCoef<T> e;
-    const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, s, ss, e);
+    const C_t<T> au = apply_row<T, C, W>(L, u, cells, G, wmu, P, s, ss, e);
     r = csub<T>(r, au);
   }
   if (rout) rout[o] = mk<TO>((TO)r.x, (TO)r.y);
@@ -155,7 +155,7 @@ __device__ __forceinline__ T residual_comp(const LevelView<T>& L, const C_t<T>* 
 
 // a thread per (component, slot), the component = blockIdx.z: one edge
 // equation per thread keeps more independent loads in flight than three
-template <typename T, typename TO>
+template <typename T, typename TO, int W>
 __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __restrict__ rout,
                                                   double* __restrict__ norm2) {
   const int rhs = blockIdx.y;
@@ -174,9 +174,9 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
     const T wmu = L.wmu[rhs];
     C_t<TO>* ro = rout ? rout + (long)rhs * 3 * L.S : nullptr;
     switch (blockIdx.z) {
-      case 0: acc = residual_comp<T, TO, 0>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
-      case 1: acc = residual_comp<T, TO, 1>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
-      default: acc = residual_comp<T, TO, 2>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
+      case 0: acc = residual_comp<T, TO, 0, W>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
+      case 1: acc = residual_comp<T, TO, 1, W>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
+      default: acc = residual_comp<T, TO, 2, W>(L, u, f, cells, G, wmu, P, s, ss, ro); break;
     }
   }
   if (norm2) block_add_t<T>(acc, norm2 + rhs);
@@ -185,7 +185,10 @@ __global__ void __launch_bounds__(256) k_residual(LevelView<T> L, C_t<TO>* __res
 template <typename T, typename TO>
 void launch_residual(const LevelView<T>& L, C_t<TO>* rout, double* norm2, cudaStream_t st) {
   dim3 grid((unsigned)((L.S + 255) / 256), L.nrhs, 3);
-  k_residual<T, TO><<<grid, 256, 0, st>>>(L, rout, norm2);
+  if (L.imu_vol)
+    k_residual<T, TO, 1><<<grid, 256, 0, st>>>(L, rout, norm2);
+  else
+    k_residual<T, TO, 0><<<grid, 256, 0, st>>>(L, rout, norm2);
 }
 
 // ------------------------------------------------------------ stored FP64 coefficients
@@ -467,7 +470,7 @@ __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>
     const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
     r = csub<T>(f[C * (int)L.S + sl], au);
   } else {
-    edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
+    edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e, L.imu_vol);
   }
   T band[5] = {0, 0, 0, 0, 0};
 #define LINE_ENTRY(K)                                                         \
@@ -752,7 +755,7 @@ __global__ void __launch_bounds__(256) k_line_apply(LevelView<T> L, int pa, int 
 // order as k_line_solve, so the same result, with 8 instead of 48 bytes per
 // row written by the assembly and no complex reciprocal per row.
 
-template <typename T, int D, int TT, int C>
+template <typename T, int D, int TT, int C, int W>
 __device__ __forceinline__ C_t<T> row_residual(const LevelView<T>& L, const C_t<T>* u,
                                                const C_t<T>* f, const T* cells,
                                                const Geo<T>& G, T wmu, int ta, int tb, int s,
@@ -764,14 +767,14 @@ __device__ __forceinline__ C_t<T> row_residual(const LevelView<T>& L, const C_t<
   P[B] = tb - (TT == 3 ? 1 : 0);
   const int sl = P[0] + (L.n[0] + 1) * (P[1] + (L.n[1] + 1) * P[2]);  // 32-bit slot
   EdgeCoef<T> e;
-  const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
+  const C_t<T> au = apply_row<T, C, W>(L, u, cells, G, wmu, P, sl, ss, e);
   return csub<T>(f[C * (int)L.S + sl], au);
 }
 
 // rb[rhs][row][line] = residual of every row of one colour; y and z lines:
 // a thread per (line, node) and its five rows; x lines: a thread per
 // (row type, line, node), row type slowest
-template <typename T, int D>
+template <typename T, int D, int W>
 __global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb, LineDiv dv,
                                                   C_t<T>* __restrict__ rb) {
   constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
@@ -803,19 +806,19 @@ __global__ void __launch_bounds__(256) k_line_rhs(LevelView<T> L, int pa, int pb
   auto put = [&](int row, C_t<T> v) { out[(long)row * g.nl] = v; };
   if (D == 0) {
     switch (rt) {
-      case 0: put(r0, row_residual<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
-      case 1: put(r0 + 1, row_residual<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
-      case 2: put(r0 + 2, row_residual<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
-      case 3: put(r0 + 3, row_residual<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
-      default: put(r0 + 4, row_residual<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 0: put(r0, row_residual<T, D, 0, D, W>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 1: put(r0 + 1, row_residual<T, D, 1, A, W>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 2: put(r0 + 2, row_residual<T, D, 2, A, W>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      case 3: put(r0 + 3, row_residual<T, D, 3, B, W>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
+      default: put(r0 + 4, row_residual<T, D, 4, B, W>(L, u, f, cells, G, wmu, ta, tb, s, ss)); break;
     }
   } else {
-    put(r0, row_residual<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+    put(r0, row_residual<T, D, 0, D, W>(L, u, f, cells, G, wmu, ta, tb, s, ss));
     if (s < g.nd) {
-      put(r0 + 1, row_residual<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, ss));
-      put(r0 + 2, row_residual<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, ss));
-      put(r0 + 3, row_residual<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, ss));
-      put(r0 + 4, row_residual<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 1, row_residual<T, D, 1, A, W>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 2, row_residual<T, D, 2, A, W>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 3, row_residual<T, D, 3, B, W>(L, u, f, cells, G, wmu, ta, tb, s, ss));
+      put(r0 + 4, row_residual<T, D, 4, B, W>(L, u, f, cells, G, wmu, ta, tb, s, ss));
     }
   }
 }
@@ -1288,7 +1291,10 @@ static void line_sweep_fac_d(const LevelView<T>& L, int color, const T* fac, con
   const int rt = sh.rhs_threads == 128 ? 128 : 256;
   dim3 gr((unsigned)(((D == 0 ? 5 : 1) * items + rt - 1) / rt), L.nrhs);
   const LineDiv dv = line_div<D>(L.n, pa, pb);
-  k_line_rhs<T, D><<<gr, rt, 0, st>>>(L, pa, pb, dv, rb);
+  if (L.imu_vol)
+    k_line_rhs<T, D, 1><<<gr, rt, 0, st>>>(L, pa, pb, dv, rb);
+  else
+    k_line_rhs<T, D, 0><<<gr, rt, 0, st>>>(L, pa, pb, dv, rb);
   dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
   if constexpr (std::is_same<T, float>::value) {
     if (fmt == kFacF16) {

@@ -131,7 +131,8 @@ __global__ void __launch_bounds__(256) k_ls_input(LevelView<float> L, const floa
     EdgeCoef<float> e;
     float2 r;
     if (rin) {
-      edge_coef<float, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e);
+      edge_coef<float, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e,
+                          L.imu_vol);
       r = rin[((long)b * 3 + C) * L.S + s];
     } else {
       const float2 au = apply_row<float, C>(L, u, cells, G, wmu, P, s, ss, e);

@@ -91,6 +91,15 @@ void stagger(int n, const double* x, double* xs, double* d, double* ds) {
 // ------------------------------------------------------------ setup kernels
 // cells64 = raw * vol, vol = d1s*d2s*d3s (gmg.c:1795-1799); sigmas floored at
 // `floor` (invmur untouched); also writes a float copy when c32 != null.
+// *flag = 1 where an operator's raw invmur (array 3 of [op][4][ncell]) is not
+// exactly 1
+__global__ void k_not_one(const float* __restrict__ raw, long ncell, int* __restrict__ flag) {
+  const float* imu = raw + ((long)blockIdx.y * 4 + 3) * ncell;
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < ncell;
+       c += (long)gridDim.x * blockDim.x)
+    if (imu[c] != 1.0f) *flag = 1;
+}
+
 __global__ void k_weight_cells(const float* __restrict__ raw, const double* __restrict__ geo,
                                int gstride, int gmax1, int n0, int n1, int n2, double floor,
                                double* __restrict__ c64, float* __restrict__ c32) {
@@ -327,6 +336,7 @@ LevelView<float> emmi_solver::view<float>(int h, int l) const {
   V.wmu = d_wmu32;
   V.active = d_active;
   V.op = d_op;
+  V.imu_vol = imu_vol ? 1 : 0;
   set_slot_divs(V);
   return V;
 }
@@ -1017,6 +1027,19 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
     CKS(cudaMemcpyAsync(raw, P->cells, (size_t)s->nop * 4 * nc0 * sizeof(float),
                         cells_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->st));
     s->raw_cells = raw;
+    if (mixed) {
+      // is every operator's invmur exactly 1 (the front end's value)?
+      int* d_flag = nullptr;
+      TRY(s->alloc((void**)&d_flag, sizeof(int)));
+      CKS(cudaMemsetAsync(d_flag, 0, sizeof(int), s->st));
+      dim3 gc(blocks_for(nc0), s->nop);
+      k_not_one<<<gc, 256, 0, s->st>>>(raw, nc0, d_flag);
+      int flag = 1;
+      CKS(cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+      CKS(cudaStreamSynchronize(s->st));
+      s->release(d_flag);
+      s->imu_vol = flag == 0;
+    }
     // survey grids in float as emf_t holds them (regrid_init_free.c:21-34)
     {
       std::vector<float> sg((size_t)s->nop * s->gstride, 0.f);
@@ -1617,6 +1640,7 @@ size_t emmi_solver_device_bytes(const emmi_solver* s) { return s ? s->bytes : 0;
 int emmi_solver_line_factor_format(const emmi_solver* s) {
   return s && s->fac_on ? s->fac_fmt : -1;
 }
+int emmi_solver_geometric_weights(const emmi_solver* s) { return s && s->imu_vol ? 1 : 0; }
 int emmi_solver_line_format(const emmi_solver* s) {
   return s && (s->opt.line_sweep || s->opt.fused_level < s->lmax) ? s->lfmt : -1;
 }

@@ -100,6 +100,9 @@ struct emmi_solver {
   // for MIXED with line_factors = 2), the device flag an fp16 multiplier out
   // of range sets, and lines per block per (level, direction)
   int lfmt = 0;
+  // every operator's input invmur is exactly 1: the complex64 operator takes
+  // its coefficients from the spacings (LevelView::imu_vol)
+  bool imu_vol = false;
   int* d_lovf = nullptr;
   int fused_nt[emmi::kMaxLev][3];
 

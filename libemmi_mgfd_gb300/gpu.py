@@ -334,6 +334,12 @@ class Solver:
         return lib().emmi_solver_line_factor_format(self._h)
 
     @property
+    def geometric_weights(self) -> bool:
+        """True when the complex64 operator forms its coefficients from the
+        mesh spacings (every input invmur exactly 1)."""
+        return bool(lib().emmi_solver_geometric_weights(self._h))
+
+    @property
     def line_format(self) -> int:
         """Multipliers of the one-launch line sweep: 1 fp16, 0 working
         precision, -1 the three-launch sweep."""

@@ -510,3 +510,35 @@ def test_fp64_stored_line_factors_give_the_same_iterates(golden):
     for r in range(3):
         assert rel_err(out[1][0][r], out[0][0][r], sea) < 1e-10
         assert rel_err(out[1][1][r], out[0][1][r]) < 1e-10
+
+
+@gpu
+def test_geometric_cell_weights_match_the_stored_ones(golden):
+    """With every invmur exactly 1 (the front end's value) the complex64
+    operator forms its coefficients from the spacings; one invmur of
+    1 + 2^-23 makes it read the stored volume-weighted cells instead.  The
+    two operators differ by float rounding (and that one cell), so six
+    mixed cycles of three RHS agree to 1e-5 below the sea surface and in
+    H; the FP64 refinement keeps the true operator in both."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    bs = np.stack([g["b_f0"], g["badj_f0"], g["b_f0"]])
+    oms = np.array([om, om, 0.5 * om], np.float32)
+    out = {}
+    for name in ("ones", "stored"):
+        r = raw.copy()
+        if name == "stored":
+            r[3].reshape(-1)[0] = np.float32(1.0) + np.float32(2.0 ** -23)
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], r[None], oms,
+                     op=np.zeros(3, np.int32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=6, tol=0.0,
+                                       sigma_floor=2e-4))
+        x, h, st = s.solve(bs)
+        out[name] = (x, h, s.geometric_weights)
+        s.close()
+    assert out["ones"][2] and not out["stored"][2]
+    sea = below_sea_mask(n, g["x3"])
+    for r in range(3):
+        assert rel_err(out["ones"][0][r], out["stored"][0][r], sea) < 1e-5
+        assert rel_err(out["ones"][1][r], out["stored"][1][r]) < 1e-5
