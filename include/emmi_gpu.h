@@ -96,6 +96,20 @@ typedef struct {
                        launches are short); levels above it the three-launch
                        sweep.  A value >= the number of levels keeps the
                        three-launch sweep everywhere                      */
+  int staged;       /* MIXED: 1 = the complex64 residual stages each plane's
+                       halo in shared memory with tensor copies (default);
+                       0 = the plain residual                              */
+  int skip_pre;     /* bit l set: level l leaves out its pre-smoothing (0:
+                       every level smooths v1 times, as the reference)     */
+  int skip_post;    /* bit l set: level l leaves out its post-smoothing (0:
+                       every level smooths v2 times, as the reference);
+                       bit 0 makes the learned correction, applied after
+                       every cycle, take the place of the last level-0
+                       post-smoothing (collect its training residuals with
+                       the same setting)                                   */
+  int learned_cycles; /* MIXED with a learned correction: apply it after the
+                       first k cycles (FGMRES: preconditioner applications)
+                       only; 0 = after every cycle (0)                     */
 } emmi_options;
 
 typedef struct {

@@ -22,7 +22,8 @@ BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 GPU_SOURCES = ["emmi_kernels.cu", "emmi_solver.cu", "emmi_survey.cu", "emmi_dropin.cu",
-               "emmi_krylov.cu", "emmi_learned.cu", "emmi_noalloc.cu", "emmi_frontend.cu"]
+               "emmi_krylov.cu", "emmi_learned.cu", "emmi_noalloc.cu", "emmi_frontend.cu",
+               "emmi_stencil.cu"]
 HOST_SOURCES = ["emmi_host.c", "emmi_fwi.c"]
 GPU_LIB = os.path.join(HERE, "libemmi_gpu.so")
 HOST_LIB = os.path.join(HERE, "libemmi_host.so")

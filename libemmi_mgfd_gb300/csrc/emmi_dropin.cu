@@ -153,6 +153,9 @@ void emmi_dropin_options(emmi_options* o, int verb) {
   o->isemicoarsen = (int)param("isemicoarsen", 1, true);
   o->precision = (int)param("gmg_precision", EMMI_PREC_MIXED, true);
   o->sigma_floor = param("sigma_floor", 0.0, false);
+  // level masks of left-out smoothing (0: the reference's cycle)
+  o->skip_pre = (int)param("skip_pre", 0, true);
+  o->skip_post = (int)param("skip_post", 0, true);
   o->verb = verb;
 }
 

@@ -1,5 +1,7 @@
 // Host-side launchers for the multigrid kernels (emmi_kernels.cu).
 #pragma once
+#include <cuda.h>
+
 #include "emmi_common.cuh"
 
 namespace emmi {
@@ -72,6 +74,32 @@ long line_l_bytes(const int n[3], int d, int color, int lf, int tsize);
 template <typename T>
 void launch_line_fused(const LevelView<T>& L, int d, int color, void* lbuf, int lf, int nt,
                        int* ovf, cudaStream_t st);
+
+// complex64 residual with its halos staged by tensor copies (emmi_stencil.cu):
+// tiles of TY rows x KZ planes, plane windows in a ring of shared-memory
+// slots.  stencil_prepare sizes the tiles and encodes the tensor maps of a
+// level's u (u_elems complex values) and cells (cell_elems floats), both
+// allocated in whole 256-byte rows (stencil_pad); false when the level
+// cannot be staged, and the plain residual is used.  stencil_err: the word a
+// staged launch whose wait ran out sets (nonzero).
+struct StencilArgs {
+  int TY, KZ;       // rows and planes of a tile
+  int ntj, ntk;     // tiles along y and z
+  int Ru, Rc;       // 256-byte rows of a u window and of a cell window
+  int ncarr;        // cell arrays staged: 3 (sigma) or 4 (+ inverse permeability)
+  unsigned uwin, cwin, slot;  // bytes: one u window, one cell window, one slot
+  long long wait;   // clocks a wait gives up after
+};
+struct StencilPlan {
+  CUtensorMap tu, tc;
+  StencilArgs args;
+  bool ok = false;
+};
+long stencil_pad(long elems, int esize);
+bool stencil_prepare(const LevelView<float>& V, long u_elems, long cell_elems, StencilPlan* out);
+void launch_residual_staged(const LevelView<float>& L, const StencilPlan& P, C_t<float>* rout,
+                            double* norm2, cudaStream_t st);
+int* stencil_err();
 
 template <typename T>
 void launch_point_sweep(const LevelView<T>& L, int color, cudaStream_t st);

@@ -4,7 +4,7 @@
  *             dx=.. dy=.. dz=.. ox=.. oy=.. [oz=0] [n1=n2=n3=128]
  *             frho11=.. frho22=.. frho33=.. fsrc=.. frec=.. fsrcrec=..
  *             [shots=1,2,..] [cycleopt ncycle v1 v2 tol isemicoarsen]
- *             [gmg_precision=1] [verb=1]
+ *             [gmg_precision=1] [skip_pre=0 skip_post=0] [verb=1]
  *   emmi_main mode=2 ... fbathy=.. [npar=2 idxpar=1,2 preco=1 addnoise=1
  *             amp_perc=0.03 delta_phi=0 noisefloorE=1e-15 noisefloorH=1e-13
  *             dsmute=800 drmute=200 gamma1=10 gamma2=0 r1=r2=r3=3 repeat=1]

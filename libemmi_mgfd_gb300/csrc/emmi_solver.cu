@@ -406,13 +406,26 @@ void emmi_solver::emit_smooth(int h, int l, int iter) {
   }
 }
 
+// r = f - A u of level l of hierarchy h (view V): the staged kernel where
+// the level has a plan, else the plain one
+template <typename T>
+void emmi_solver::resid(int h, int l, const LevelView<T>& V, C_t<T>* rout, double* norm2) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (plan[h][l].ok) {
+      launch_residual_staged(V, plan[h][l], rout, norm2, st);
+      return;
+    }
+  }
+  launch_residual<T, T>(V, rout, norm2, st);
+}
+
 // level-0 residual with norm: the point where the cycle tests convergence
 template <typename T>
 void emmi_solver::emit_residual0(int want, int& cur) {
   if (cur == want) {
     cudaMemsetAsync(d_norm, 0, nrhs * sizeof(double), st);
     LevelView<T> V = view<T>(0, 0);
-    launch_residual<T, T>(V, V.r, d_norm, st);
+    resid<T>(0, 0, V, V.r, d_norm);
     launch_counter++;
   }
   cur = 1;
@@ -442,7 +455,7 @@ void emmi_solver::emit_cycle(int h, int l, int kind, int want, int& cur) {
       emit_residual0<T>(want, cur);
     } else if (cur == want) {
       LevelView<T> V = view<T>(h, lv);
-      launch_residual<T, T>(V, V.r, nullptr, st);
+      resid<T>(h, lv, V, V.r, nullptr);
       launch_counter++;
     }
   };
@@ -465,8 +478,10 @@ void emmi_solver::emit_cycle(int h, int l, int kind, int want, int& cur) {
     emit_cycle<T>(h, l, 1, want, cur);
     return;
   }
-  // V (kind 1) and W (kind 3)
-  for (int i = 0; i < opt.v1; i++) smooth(l, i);
+  // V (kind 1) and W (kind 3); levels whose bit is set in skip_pre /
+  // skip_post leave out that smoothing
+  if (!((opt.skip_pre >> l) & 1))
+    for (int i = 0; i < opt.v1; i++) smooth(l, i);
   if (can_descend(l)) {
     residual(l);
     to_coarse(l);
@@ -474,7 +489,8 @@ void emmi_solver::emit_cycle(int h, int l, int kind, int want, int& cur) {
     if (kind == 3) emit_cycle<T>(h, l + 1, kind, want, cur);
     to_fine(l);
   }
-  for (int i = 0; i < opt.v2; i++) smooth(l, i);
+  if (!((opt.skip_post >> l) & 1))
+    for (int i = 0; i < opt.v2; i++) smooth(l, i);
 }
 
 template <typename T>
@@ -832,6 +848,10 @@ void emmi_default_options(emmi_options* o) {
   o->autotune = 1;
   o->line_sweep = 0;
   o->fused_level = 99;
+  o->staged = 1;
+  o->skip_pre = 0;
+  o->skip_post = 0;
+  o->learned_cycles = 0;
 }
 
 static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
@@ -1108,7 +1128,8 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
       TRY(s->alloc((void**)&base, (size_t)s->nop * 4 * nc0 * sizeof(double)));
       TRY(s->alloc((void**)&pp[0], (size_t)s->nop * 4 * nc0 * sizeof(double)));
       TRY(s->alloc((void**)&pp[1], (size_t)s->nop * 4 * nc0 * sizeof(double)));
-      TRY(s->alloc((void**)&s->cells32[0][0], (size_t)s->nop * 4 * nc0 * sizeof(float)));
+      TRY(s->alloc((void**)&s->cells32[0][0],
+                   (size_t)stencil_pad((long)s->nop * 4 * nc0, 4) * sizeof(float)));
       k_weight_cells<<<g0, 256, 0, s->st>>>(raw, s->geo64[0][0], s->gstride, s->gmax1, s->n[0],
                                             s->n[1], s->n[2], floor, base, s->cells32[0][0]);
       for (int h = 1; h < 3; h++) s->cells32[h][0] = s->cells32[0][0];
@@ -1118,7 +1139,8 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
           const HLev& C = s->hier[h][l];
           double* dst = pp[l & 1];
           launch_coarsen_cells<double>(src, s->hier[h][l - 1].n, dst, C.sc, s->nop, s->st);
-          TRY(s->alloc((void**)&s->cells32[h][l], (size_t)s->nop * 4 * C.ncell * sizeof(float)));
+          TRY(s->alloc((void**)&s->cells32[h][l],
+                       (size_t)stencil_pad((long)s->nop * 4 * C.ncell, 4) * sizeof(float)));
           const long nn = (long)s->nop * 4 * C.ncell;
           k_d2f<<<blocks_for(nn), 256, 0, s->st>>>(dst, s->cells32[h][l], nn);
           src = dst;
@@ -1144,9 +1166,12 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
         if (!mixed) TRY(s->alloc((void**)&s->r64[l], n3 * sizeof(double2)));
       }
       if (mixed) {
-        TRY(s->alloc((void**)&s->u32[l], n3 * sizeof(float2)));
-        TRY(s->alloc((void**)&s->f32[l], n3 * sizeof(float2)));
-        TRY(s->alloc((void**)&s->r32[l], n3 * sizeof(float2)));
+        // whole 256-byte rows: the staged residual's tensor maps read them
+        const size_t n3p = (size_t)stencil_pad((long)n3, 8);
+        TRY(s->alloc((void**)&s->u32[l], n3p * sizeof(float2)));
+        TRY(s->alloc((void**)&s->f32[l], n3p * sizeof(float2)));
+        TRY(s->alloc((void**)&s->r32[l], n3p * sizeof(float2)));
+        s->u32_elems[l] = (long)n3;
       }
     }
     // line-sweep scratch: largest (level, direction) over the hierarchies,
@@ -1190,6 +1215,14 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
       }
     }
     mark("sweep shapes");
+    if (mixed && s->opt.staged) {
+      // staged residual on level 0 (shared by the hierarchies); the coarse
+      // levels are too small to fill the GPU with plane-marching tiles and
+      // sit in L2, where the plain residual is faster
+      LevelView<float> V = s->view<float>(0, 0);
+      if (stencil_prepare(V, s->u32_elems[0], (long)s->nop * 4 * V.ncell, &s->plan[0][0]))
+        for (int h = 1; h < 3; h++) s->plan[h][0] = s->plan[0][0];
+    }
     if (mixed) TRY(build_coef64(s));
     mark("FP64 coefficients");
   }
@@ -1259,7 +1292,16 @@ static int upload_mask(emmi_solver* s, int* dev, const std::vector<int>& host) {
 
 static int read_norms(emmi_solver* s, const double* dev, std::vector<double>& host) {
   CK(cudaMemcpyAsync(host.data(), dev, host.size() * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  int staged_err = 0;
+  if (s->opt.staged)
+    CK(cudaMemcpyAsync(&staged_err, stencil_err(), sizeof(int), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
+  if (staged_err) {
+    cudaMemsetAsync(stencil_err(), 0, sizeof(int), s->st);
+    cudaStreamSynchronize(s->st);
+    set_err("a staged residual's wait for its tensor copies ran out");
+    return EMMI_ECUDA;
+  }
   return EMMI_OK;
 }
 
@@ -1346,7 +1388,7 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
           dim3 g(blocks_for(n3s, 256, 2048), nrhs);
           k_zero_masked<<<g, 256, 0, s->st>>>(s->u32[0], n3s, s->d_active);
           LevelView<float> R = s->view<float>(hh, 0);
-          launch_residual<float, float>(R, R.r, nullptr, s->st);
+          s->resid<float>(hh, 0, R, R.r, nullptr);
           s->last_launches += 2;
           for (int r = 0; r < nrhs; r++) since[r] = 0;
           rc = EMMI_OK;
@@ -1412,13 +1454,15 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
             if ((rc = upload_mask(s, s->d_refine, ref)) != EMMI_OK) return rc;
             LevelView<float> R = s->view<float>(hh, 0);
             R.active = s->d_refine;
-            launch_residual<float, float>(R, R.r, nullptr, s->st);
+            s->resid<float>(hh, 0, R, R.r, nullptr);
             s->last_launches++;
           }
         }
       }
       if ((rc = run_part(s, hh, 1)) != EMMI_OK) return rc;
-      if (s->learned_on && (rc = learned_after_cycle(s, hh, act)) != EMMI_OK) return rc;
+      if (s->learned_on && (s->opt.learned_cycles <= 0 || icycle < s->opt.learned_cycles) &&
+          (rc = learned_after_cycle(s, hh, act)) != EMMI_OK)
+        return rc;
       if (s->ls_collect && (rc = learned_snapshot(s, hh, act)) != EMMI_OK) return rc;
       for (int r = 0; r < nrhs; r++)
         if (act[r]) {

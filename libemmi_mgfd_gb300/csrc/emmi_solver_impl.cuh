@@ -52,6 +52,10 @@ struct emmi_solver {
   float* cells32[3][emmi::kMaxLev] = {};
   double2 *u64[emmi::kMaxLev] = {}, *f64[emmi::kMaxLev] = {}, *r64[emmi::kMaxLev] = {};
   float2 *u32[emmi::kMaxLev] = {}, *f32[emmi::kMaxLev] = {}, *r32[emmi::kMaxLev] = {};
+  long u32_elems[emmi::kMaxLev] = {};  // complex values of u32[l] (before padding)
+  // staged residual (opt.staged, MIXED): tile plans and tensor maps per
+  // (hierarchy, level); ok false where a level cannot be staged
+  emmi::StencilPlan plan[3][emmi::kMaxLev];
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
   int chunk = 1;  // RHS per line-sweep launch (scratch bound)
@@ -149,6 +153,8 @@ struct emmi_solver {
 
   template <typename T> emmi::LevelView<T> view(int h, int l) const;
   template <typename T> void emit_smooth(int h, int l, int iter);
+  template <typename T>
+  void resid(int h, int l, const emmi::LevelView<T>& V, emmi::C_t<T>* rout, double* norm2);
   template <typename T> void emit_cycle(int h, int l, int kind, int want, int& cur);
   template <typename T> void emit_residual0(int want, int& cur);
   template <typename T> int build_graphs();

@@ -96,14 +96,18 @@ def make_solver(p: Dict, **opt) -> G.Solver:
 
 
 def train(n: int = 48, models: int = 6, per_rhs: int = 6, steps: int = 300, lr: float = 3e-3,
-          seed: int = 100, weights=None) -> Dict:
+          seed: int = 100, weights=None, skip_post: int = 0) -> Dict:
     """Collect residual samples of plain complex64 cycles on `models` random
     surveys and train the network on them with full-batch Adam on the GPU.
     Returns the weights, the loss history (mean |r - A c|^2/|r|^2, 1.0 for
-    the zero correction) and the seconds spent."""
+    the zero correction) and the seconds spent.  skip_post: the cycles
+    whose residuals are collected leave out the post-smoothing of the levels
+    whose bit is set (emmi_options.skip_post; bit 0 puts the correction in
+    the place of the level-0 post-smoothing)."""
     t0 = time.perf_counter()
     p = training_problem(n, models, seed)
-    s = make_solver(p, precision=G.PREC_MIXED, tol=1e-8, ncycle=per_rhs + 4)
+    s = make_solver(p, precision=G.PREC_MIXED, tol=1e-8, ncycle=per_rhs + 4,
+                    skip_post=skip_post)
     b = s.inject_sources(p["src"])
     st = s.learned_collect(b.data_ptr(), per_rhs, device=True)
     t1 = time.perf_counter()

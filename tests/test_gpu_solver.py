@@ -542,3 +542,67 @@ def test_geometric_cell_weights_match_the_stored_ones(golden):
     for r in range(3):
         assert rel_err(out["ones"][0][r], out["stored"][0][r], sea) < 1e-5
         assert rel_err(out["ones"][1][r], out["stored"][1][r]) < 1e-5
+
+
+@gpu
+@pytest.mark.parametrize("case", ["tiny_layered", "tiny_aniso", "c1_layered_64"])
+def test_staged_residual_gives_the_plain_iterates(golden, case):
+    """The complex64 residual with its halos staged in shared memory by
+    tensor copies (tiles of rows x 32 planes, the default) against the plain
+    residual: the same edge equations, so six mixed cycles give the same
+    iterates to rounding (the norms add in another order; the refinement
+    points are the same).  The cases cover one and several plane chunks,
+    a non-cubic grid and partial row tiles."""
+    g = golden(case)
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    b = g["b_f0"] if "b_f0" in g else None
+    if b is None:
+        src = g["srcrec"][:5]
+        b = O.inject_source(_grid(g), src, str(g["chsrc"]).split(","), om)
+    out = {}
+    for staged in (1, 0):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None],
+                     np.array([om], np.float32),
+                     options=G.Options(precision=G.PREC_MIXED, ncycle=6, tol=0.0,
+                                       sigma_floor=2e-4, staged=staged))
+        x, h, st = s.solve(b[None])
+        out[staged] = (x, h, st[0]["cycles"])
+        s.close()
+    assert out[1][2] == out[0][2] == 6
+    sea = below_sea_mask(n, g["x3"])
+    assert rel_err(out[1][0][0], out[0][0][0], sea) < 1e-6
+    assert rel_err(out[1][1][0], out[0][1][0]) < 1e-6
+
+
+@gpu
+@pytest.mark.parametrize("precision", [1, 0])
+def test_skipped_post_smoothing_converges_to_the_same_field(golden, precision):
+    """emmi_options.skip_post = 3 (no post-smoothing on levels 0 and 1): a
+    weaker cycle with fewer launches, run to the same tolerance as the
+    reference's cycle; the fields agree to the tolerance's order below the
+    sea, every level's launches of the left-out smoothing are gone from the
+    cycle, and skip_post = 0 is the reference's cycle (the other tests)."""
+    g = golden("c1_layered_64")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    b = g["b_f0"] if "b_f0" in g else None
+    if b is None:
+        src = g["srcrec"][:5]
+        b = O.inject_source(_grid(g), src, str(g["chsrc"]).split(","), om)
+    out = {}
+    for mask in (0, 3):
+        s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None],
+                     np.array([om], np.float32),
+                     options=G.Options(precision=precision, ncycle=60, tol=1e-8,
+                                       skip_post=mask))
+        x, h, st = s.solve(b[None])
+        out[mask] = (x, h, st[0], s.last_launches)
+        s.close()
+    for mask in (0, 3):
+        assert out[mask][2]["status"] == "ok" and out[mask][2]["rel"] <= 1e-8, out[mask][2]
+    sea = below_sea_mask(n, g["x3"])
+    assert rel_err(out[3][0][0], out[0][0][0], sea) < 1e-5
+    # fewer launches per cycle without the two levels' post-smoothing
+    per = {m: out[m][3] / out[m][2]["cycles"] for m in (0, 3)}
+    assert per[3] < per[0], per
