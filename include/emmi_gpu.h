@@ -107,9 +107,6 @@ typedef struct {
                        every cycle, take the place of the last level-0
                        post-smoothing (collect its training residuals with
                        the same setting)                                   */
-  int learned_cycles; /* MIXED with a learned correction: apply it after the
-                       first k cycles (FGMRES: preconditioner applications)
-                       only; 0 = after every cycle (0)                     */
 } emmi_options;
 
 typedef struct {

@@ -365,9 +365,7 @@ int krylov_solve(emmi_solver* s, std::vector<int>& cycles, std::vector<int>& sta
     const int hh_ = s->opt.isemicoarsen ? app % 3 : 0;
     if ((rc = run_part(s, hh_, 0)) != EMMI_OK) return rc;
     if ((rc = run_part(s, hh_, 1)) != EMMI_OK) return rc;
-    if (s->learned_on && (s->opt.learned_cycles <= 0 || app < s->opt.learned_cycles) &&
-        (rc = learned_after_cycle(s, hh_, act)) != EMMI_OK)
-      return rc;
+    if (s->learned_on && (rc = learned_after_cycle(s, hh_, act)) != EMMI_OK) return rc;
     k_kry_store<<<g, 256, 0, st>>>(s->u32[0], s->kz, s->kt, s->d_kj, n3s, nrhs, s->d_active);
     // w = A z_j = 0 - A (-z_j), FP64
     LevelView<double> V = s->view<double>(0, 0);

@@ -851,7 +851,6 @@ void emmi_default_options(emmi_options* o) {
   o->staged = 1;
   o->skip_pre = 0;
   o->skip_post = 0;
-  o->learned_cycles = 0;
 }
 
 static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_options* opts,
@@ -1460,9 +1459,7 @@ static int solve_impl(emmi_solver* s, const double* b, double* x, double* h, int
         }
       }
       if ((rc = run_part(s, hh, 1)) != EMMI_OK) return rc;
-      if (s->learned_on && (s->opt.learned_cycles <= 0 || icycle < s->opt.learned_cycles) &&
-          (rc = learned_after_cycle(s, hh, act)) != EMMI_OK)
-        return rc;
+      if (s->learned_on && (rc = learned_after_cycle(s, hh, act)) != EMMI_OK) return rc;
       if (s->ls_collect && (rc = learned_snapshot(s, hh, act)) != EMMI_OK) return rc;
       for (int r = 0; r < nrhs; r++)
         if (act[r]) {

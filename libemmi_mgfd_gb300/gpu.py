@@ -53,7 +53,7 @@ class _Options(C.Structure):
                 ("use_graphs", C.c_int), ("verb", C.c_int), ("krylov", C.c_int),
                 ("line_factors", C.c_int), ("autotune", C.c_int), ("line_sweep", C.c_int),
                 ("fused_level", C.c_int), ("staged", C.c_int), ("skip_pre", C.c_int),
-                ("skip_post", C.c_int), ("learned_cycles", C.c_int)]
+                ("skip_post", C.c_int)]
 
 
 class _Stats(C.Structure):
@@ -114,14 +114,13 @@ class Options:
     staged: int = 1
     skip_pre: int = 0
     skip_post: int = 0
-    learned_cycles: int = 0
 
     def _c(self) -> _Options:
         return _Options(self.cycleopt, self.ncycle, self.v1, self.v2, self.tol, self.isemicoarsen,
                         self.precision, self.sigma_floor, self.refine_every, self.use_graphs,
                         self.verb, self.krylov, self.line_factors, self.autotune,
                         self.line_sweep, self.fused_level, self.staged, self.skip_pre,
-                        self.skip_post, self.learned_cycles)
+                        self.skip_post)
 
 
 class Solver:
