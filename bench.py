@@ -82,6 +82,8 @@ def parse():
     p.add_argument("--no-learned", action="store_true",
                    help="plain complex64 cycles (no learned correction)")
     p.add_argument("--krylov", type=int, default=0, help="FGMRES restart length (0: refinement)")
+    p.add_argument("--no-staged", action="store_true",
+                   help="the plain complex64 residual instead of the tensor-copy staged one")
     p.add_argument("--profile", action="store_true",
                    help="one shot: a short solve, then one level-0 line sweep inside the NVTX "
                         "range emmi_profile (for ncu --nvtx-include emmi_profile/)")
@@ -289,14 +291,16 @@ def parity_report(w, d, a):
     return out
 
 
-def make_solver(w, precision, tol, krylov=0, ncycle=100, line_factors=2, skip_post=SKIP_POST):
+def make_solver(w, precision, tol, krylov=0, ncycle=100, line_factors=2, skip_post=SKIP_POST,
+                staged=1):
     from libemmi_mgfd_gb300 import gpu as G
     n = w["survey"].n
     nrhs = w["X1"].shape[0]
     return G.Solver(n, w["X1"], w["X2"], w["X3"], w["cells"], w["omega"],
                     op=np.arange(nrhs, dtype=np.int32),
                     options=G.Options(precision=precision, tol=tol, ncycle=ncycle, krylov=krylov,
-                                      line_factors=line_factors, skip_post=skip_post),
+                                      line_factors=line_factors, skip_post=skip_post,
+                                      staged=staged),
                     rho_water=w["rho_water"])
 
 
@@ -507,7 +511,7 @@ def main():
                    "loss_start": round(float(tr["loss"][0]), 4),
                    "loss_end": round(float(tr["loss"][-1]), 4)}
 
-    solver = make_solver(w, G.PREC_MIXED, a.tol, krylov=a.krylov)
+    solver = make_solver(w, G.PREC_MIXED, a.tol, krylov=a.krylov, staged=0 if a.no_staged else 1)
     shapes, _ = solver.sweep_shapes()
     if W is not None:
         solver.set_learned(W)
