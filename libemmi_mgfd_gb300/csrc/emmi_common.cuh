@@ -95,6 +95,11 @@ template <typename T> struct LevelView {
   // coefficients come from the spacings alone (edge_coef); set only for the
   // complex64 preconditioner operator
   int imu_vol = 0;
+  // [op][3][gmax1]: weight wr of every fine node index along each axis for
+  // the transfer to the next coarser level, (x_f[F] - x_c[c]) / (x_c[c+1] -
+  // x_c[c]) with c the coarse interval of F (k_xfer_weights); null on the
+  // coarsest level
+  const T* xw = nullptr;
 };
 
 // the slot-decode divisors of a view, set on the host wherever a view is built

@@ -1863,67 +1863,99 @@ struct Xfer {
   int nf[3], nc[3], sc[3];
 };
 
-// fine indices and weights contributing to coarse transverse index Ce along e
+// the transfer weights of a level (LevelView::xw), once per set-up: the
+// arithmetic the transfers used to repeat in every thread
 template <typename T>
-__device__ __forceinline__ int xfer_list(int Ce, int sce, int nfe, int nce, const T* xf, const T* xc,
-                                         int (&idx)[4], T (&w)[4]) {
-  int cnt = 0;
-  // left: map(F) == Ce, weight 1 - wr
-  if (Ce < nce) {
-    const T x0 = xc[Ce], h = xc[Ce + 1] - xc[Ce];
-    const int f0 = sce == 2 ? 2 * Ce : Ce;
-    for (int t = 0; t < sce; t++) {
-      const int F = f0 + t;
-      if (F >= 1 && F < nfe) {
-        idx[cnt] = F;
-        w[cnt] = T(1) - (xf[F] - x0) / h;
-        cnt++;
-      }
-    }
+__global__ void __launch_bounds__(256) k_xfer_weights(LevelView<T> F, LevelView<T> Cc, int sc0,
+                                                      int sc1, int sc2, int nop, T* __restrict__ out) {
+  const int g1 = F.gmax1;
+  const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (id >= (long)nop * 3 * g1) return;
+  const int o = (int)(id / (3 * g1));
+  const int e = (int)((id / g1) % 3);
+  const int f = (int)(id % g1);
+  const int sc = e == 0 ? sc0 : e == 1 ? sc1 : sc2;
+  const int c = sc == 2 ? f / 2 : f;
+  T w = 0;
+  if (f <= F.n[e] && c < Cc.n[e]) {
+    const T* xf = F.geo + (long)o * F.gstride + (long)e * g1;
+    const T* xc = Cc.geo + (long)o * Cc.gstride + (long)e * g1;
+    w = (xf[f] - xc[c]) / (xc[c + 1] - xc[c]);
   }
-  // right: map(F) == Ce-1, weight wr
-  if (Ce >= 1) {
-    const T x0 = xc[Ce - 1], h = xc[Ce] - xc[Ce - 1];
-    const int f0 = sce == 2 ? 2 * (Ce - 1) : Ce - 1;
-    for (int t = 0; t < sce; t++) {
-      const int F = f0 + t;
-      if (F >= 1 && F < nfe) {
-        idx[cnt] = F;
-        w[cnt] = (xf[F] - x0) / h;
-        cnt++;
-      }
-    }
+  out[id] = w;
+}
+
+template <typename T>
+void launch_xfer_weights(const LevelView<T>& F, const LevelView<T>& Cc, const int sc[3], int nop,
+                         T* out, cudaStream_t st) {
+  const long n = (long)nop * 3 * F.gmax1;
+  k_xfer_weights<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, Cc, sc[0], sc[1], sc[2], nop, out);
+}
+template void launch_xfer_weights<float>(const LevelView<float>&, const LevelView<float>&,
+                                         const int*, int, float*, cudaStream_t);
+template void launch_xfer_weights<double>(const LevelView<double>&, const LevelView<double>&,
+                                          const int*, int, double*, cudaStream_t);
+
+// the fine nodes along axis e restricted to coarse node Ce, in the order of
+// src/gmg.c:1510-1573: those whose coarse interval starts at Ce (weight
+// 1 - wr), then those whose interval ends at Ce (weight wr), two slots each;
+// a slot is used when its node is an interior fine node and its weight is
+// not exactly zero (a zero-weight term adds nothing to the sum)
+template <typename T>
+__device__ __forceinline__ void xfer_slots(int Ce, int sce, int nfe, int nce,
+                                           const T* __restrict__ wr, int (&idx)[4], T (&w)[4],
+                                           bool (&ok)[4]) {
+#pragma unroll
+  for (int t = 0; t < 2; t++) {
+    const int F = (sce == 2 ? 2 * Ce : Ce) + t;
+    idx[t] = F;
+    w[t] = T(0);
+    if (t < sce && Ce < nce && F >= 1 && F < nfe) w[t] = T(1) - ldro(wr + F);
+    ok[t] = w[t] != T(0);
   }
-  return cnt;
+#pragma unroll
+  for (int t = 0; t < 2; t++) {
+    const int F = (sce == 2 ? 2 * (Ce - 1) : Ce - 1) + t;
+    idx[2 + t] = F;
+    w[2 + t] = T(0);
+    if (t < sce && Ce >= 1 && F >= 1 && F < nfe) w[2 + t] = ldro(wr + F);
+    ok[2 + t] = w[2 + t] != T(0);
+  }
 }
 
 template <typename T, int C>
 __device__ __forceinline__ C_t<T> restrict_comp(const LevelView<T>& F, const LevelView<T>& Cc,
                                                 const int sc[3], const int Cn[3],
-                                                const C_t<T>* rf, const Geo<T>& Gf,
-                                                const Geo<T>& Gc) {
+                                                const C_t<T>* __restrict__ rf,
+                                                const T* __restrict__ xw) {
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
   constexpr int t1 = p < q ? p : q, t2 = p < q ? q : p;
   int i1[4], i2[4];
   T w1[4], w2[4];
-  const int n1c = xfer_list<T>(Cn[t1], sc[t1], F.n[t1], Cc.n[t1], Gf.x(t1), Gc.x(t1), i1, w1);
-  const int n2c = xfer_list<T>(Cn[t2], sc[t2], F.n[t2], Cc.n[t2], Gf.x(t2), Gc.x(t2), i2, w2);
+  bool o1[4], o2[4];
+  xfer_slots<T>(Cn[t1], sc[t1], F.n[t1], Cc.n[t1], xw + t1 * F.gmax1, i1, w1, o1);
+  xfer_slots<T>(Cn[t2], sc[t2], F.n[t2], Cc.n[t2], xw + t2 * F.gmax1, i2, w2, o2);
+  const int fs[3] = {1, F.n[0] + 1, (F.n[0] + 1) * (F.n[1] + 1)};
   T ar = 0, ai = 0;
   const int f0 = sc[C] == 2 ? 2 * Cn[C] : Cn[C];
-  for (int t = 0; t < sc[C]; t++) {
+#pragma unroll
+  for (int t = 0; t < 2; t++) {
     const int fc = f0 + t;
-    if (fc >= F.n[C]) continue;
-    for (int a = 0; a < n1c; a++)
-      for (int b = 0; b < n2c; b++) {
-        int P[3];
-        P[C] = fc;
-        P[t1] = i1[a];
-        P[t2] = i2[b];
-        const C_t<T> v = rf[C * (int)F.S + slot_id32(F.n, P[0], P[1], P[2])];
+    if (t >= sc[C] || fc >= F.n[C]) continue;
+    const int base = C * (int)F.S + fc * fs[C];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      if (!o1[a]) continue;
+      const int ba = base + i1[a] * fs[t1];
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        if (!o2[b]) continue;
+        const C_t<T> v = ldro(rf + (ba + i2[b] * fs[t2]));
         const T w = w1[a] * w2[b];
         ar += w * v.x;
         ai += w * v.y;
       }
+    }
   }
   return mk<T>(ar, ai);
 }
@@ -1942,13 +1974,12 @@ __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C
   const int c = blockIdx.z;  // one component per thread
   C_t<T>* fc = Cc.f + ((long)rhs * 3 + c) * Cc.S;
   C_t<T>* uc = Cc.u + ((long)rhs * 3 + c) * Cc.S;
-  const Geo<T> Gf{F.geo + (long)op_of(F, rhs) * F.gstride, F.gmax1};
-  const Geo<T> Gc{Cc.geo + (long)op_of(Cc, rhs) * Cc.gstride, Cc.gmax1};
+  const T* xw = F.xw + (long)op_of(F, rhs) * 3 * F.gmax1;
   C_t<T> v;
   switch (c) {
-    case 0: v = restrict_comp<T, 0>(F, Cc, sc, Cn, rf, Gf, Gc); break;
-    case 1: v = restrict_comp<T, 1>(F, Cc, sc, Cn, rf, Gf, Gc); break;
-    default: v = restrict_comp<T, 2>(F, Cc, sc, Cn, rf, Gf, Gc); break;
+    case 0: v = restrict_comp<T, 0>(F, Cc, sc, Cn, rf, xw); break;
+    case 1: v = restrict_comp<T, 1>(F, Cc, sc, Cn, rf, xw); break;
+    default: v = restrict_comp<T, 2>(F, Cc, sc, Cn, rf, xw); break;
   }
   fc[s] = v;
   uc[s] = mk<T>(0, 0);
@@ -1963,20 +1994,16 @@ void launch_restrict(const LevelView<T>& F, const LevelView<T>& Cc, const int sc
 template <typename T, int C>
 __device__ __forceinline__ void prolong_comp(const LevelView<T>& F, const LevelView<T>& Cc,
                                              const int sc[3], const int P[3], C_t<T>* uf,
-                                             const C_t<T>* uc, const Geo<T>& Gf, const Geo<T>& Gc,
-                                             long s) {
+                                             const C_t<T>* __restrict__ uc,
+                                             const T* __restrict__ xw, long s) {
   constexpr int p = Cyc<C>::p, q = Cyc<C>::q;
   constexpr int t1 = p < q ? p : q, t2 = p < q ? q : p;
   if (!(P[C] < F.n[C] && P[t1] >= 1 && P[t1] < F.n[t1] && P[t2] >= 1 && P[t2] < F.n[t2])) return;
   int Cn[3];
 #pragma unroll
   for (int e = 0; e < 3; e++) Cn[e] = sc[e] == 2 ? P[e] / 2 : P[e];
-  const T* xf1 = Gf.x(t1);
-  const T* xc1 = Gc.x(t1);
-  const T* xf2 = Gf.x(t2);
-  const T* xc2 = Gc.x(t2);
-  const T wr1 = (xf1[P[t1]] - xc1[Cn[t1]]) / (xc1[Cn[t1] + 1] - xc1[Cn[t1]]);
-  const T wr2 = (xf2[P[t2]] - xc2[Cn[t2]]) / (xc2[Cn[t2] + 1] - xc2[Cn[t2]]);
+  const T wr1 = ldro(xw + t1 * F.gmax1 + P[t1]);
+  const T wr2 = ldro(xw + t2 * F.gmax1 + P[t2]);
   const T wl1 = T(1) - wr1, wl2 = T(1) - wr2;
   // 32-bit offsets: the four coarse neighbours differ by the strides of t1, t2
   const int cs[3] = {1, Cc.n[0] + 1, (Cc.n[0] + 1) * (Cc.n[1] + 1)};
@@ -2003,12 +2030,11 @@ __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> Cc
   slot_nodes(s, F, P);
   C_t<T>* uf = F.u + (long)rhs * 3 * F.S;
   const C_t<T>* uc = Cc.u + (long)rhs * 3 * Cc.S;
-  const Geo<T> Gf{F.geo + (long)op_of(F, rhs) * F.gstride, F.gmax1};
-  const Geo<T> Gc{Cc.geo + (long)op_of(Cc, rhs) * Cc.gstride, Cc.gmax1};
+  const T* xw = F.xw + (long)op_of(F, rhs) * 3 * F.gmax1;
   switch (blockIdx.z) {  // one component per thread
-    case 0: prolong_comp<T, 0>(F, Cc, sc, P, uf, uc, Gf, Gc, s); break;
-    case 1: prolong_comp<T, 1>(F, Cc, sc, P, uf, uc, Gf, Gc, s); break;
-    default: prolong_comp<T, 2>(F, Cc, sc, P, uf, uc, Gf, Gc, s); break;
+    case 0: prolong_comp<T, 0>(F, Cc, sc, P, uf, uc, xw, s); break;
+    case 1: prolong_comp<T, 1>(F, Cc, sc, P, uf, uc, xw, s); break;
+    default: prolong_comp<T, 2>(F, Cc, sc, P, uf, uc, xw, s); break;
   }
 }
 

@@ -105,6 +105,10 @@ template <typename T>
 void launch_point_sweep(const LevelView<T>& L, int color, cudaStream_t st);
 
 // coarse.f = R fine.r ; coarse.u = 0
+// LevelView::xw of the transfer F -> Cc for every operator (set-up)
+template <typename T>
+void launch_xfer_weights(const LevelView<T>& F, const LevelView<T>& Cc, const int sc[3], int nop,
+                         T* out, cudaStream_t st);
 template <typename T>
 void launch_restrict(const LevelView<T>& F, const LevelView<T>& Cc, const int sc[3], cudaStream_t st);
 // fine.u += P coarse.u

@@ -307,6 +307,7 @@ LevelView<double> emmi_solver::view<double>(int h, int l) const {
   V.gstride = gstride;
   V.gmax1 = gmax1;
   V.geo = geo64[h][l];
+  V.xw = xw64[h][l];
   V.cells = cells64[h][l];
   V.u = u64[l];
   V.f = f64[l];
@@ -329,6 +330,7 @@ LevelView<float> emmi_solver::view<float>(int h, int l) const {
   V.gstride = gstride;
   V.gmax1 = gmax1;
   V.geo = geo32[h][l];
+  V.xw = xw32[h][l];
   V.cells = cells32[h][l];
   V.u = u32[l];
   V.f = f32[l];
@@ -1010,6 +1012,18 @@ static int create_impl(emmi_solver** out, const emmi_problem* P, const emmi_opti
         CKS(cudaStreamSynchronize(s->st));
       }
     }
+    // transfer weights of every level but the coarsest, from the geometry
+    const size_t wsz = (size_t)s->nop * 3 * s->gmax1;
+    for (int h = 0; h < 3; h++)
+      for (int l = 0; l + 1 < s->lmax; l++) {
+        TRY(s->alloc((void**)&s->xw64[h][l], wsz * sizeof(double)));
+        TRY(s->alloc((void**)&s->xw32[h][l], wsz * sizeof(float)));
+        launch_xfer_weights<double>(s->view<double>(h, l), s->view<double>(h, l + 1),
+                                    s->hier[h][l + 1].sc, s->nop, s->xw64[h][l], s->st);
+        launch_xfer_weights<float>(s->view<float>(h, l), s->view<float>(h, l + 1),
+                                   s->hier[h][l + 1].sc, s->nop, s->xw32[h][l], s->st);
+      }
+    CKS(cudaGetLastError());
   }
 
   // ---- per-RHS scalars

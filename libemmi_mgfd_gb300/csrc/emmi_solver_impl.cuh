@@ -48,6 +48,9 @@ struct emmi_solver {
   double* d_norm64 = nullptr;  // FP64 refinement norm^2 per RHS
   double* geo64[3][emmi::kMaxLev] = {};
   float* geo32[3][emmi::kMaxLev] = {};
+  // transfer weights of level l to l+1 per hierarchy (LevelView::xw)
+  double* xw64[3][emmi::kMaxLev] = {};
+  float* xw32[3][emmi::kMaxLev] = {};
   double* cells64[3][emmi::kMaxLev] = {};
   float* cells32[3][emmi::kMaxLev] = {};
   double2 *u64[emmi::kMaxLev] = {}, *f64[emmi::kMaxLev] = {}, *r64[emmi::kMaxLev] = {};
