@@ -402,6 +402,15 @@ int emmi_level_residual(const int n[3], const double *x1, const double *x2,
                         const double *x3, const double *cells, double omega,
                         int prec, const double *u, const double *f, double *r,
                         double *norm);
+/* one grid transfer between a level of nf cells (node coordinates x1..x3)
+ * and the level coarsened by sc (1 or 2 per direction, coordinates
+ * sub-sampled as gmg.c:1784-1786 builds them): dir 0 restricts the fine
+ * complex field in ([3][S_f]) to out ([3][S_c], gmg.c:1510-1573); dir 1 adds
+ * the prolongation of the coarse in ([3][S_c]) to out ([3][S_f],
+ * gmg.c:1463-1505) */
+int emmi_level_transfer(const int nf[3], const double *x1, const double *x2,
+                        const double *x3, const int sc[3], int prec, int dir,
+                        const double *in, double *out);
 /* one multicolour sweep: dir 0..2 = line relaxation along x/y/z,
  * dir 3 = node-patch relaxation; iter%2==1 reverses the colour order */
 int emmi_level_smooth(const int n[3], const double *x1, const double *x2,

@@ -1836,6 +1836,79 @@ int level_op(const int n[3], const double* x1, const double* x2, const double* x
   }
   return EMMI_OK;
 }
+
+// one transfer between a level of nf cells and the level coarsened by sc
+// (coordinates sub-sampled, as the hierarchy builds them): dir 0 restricts
+// the fine in to the coarse out, dir 1 adds the prolongation of the coarse
+// in to the fine out
+template <typename T>
+int level_xfer(const int nf[3], const double* const xf[3], const int sc[3], int dir,
+               const double* in, double* out) {
+  OneLevel M;
+  int nc[3];
+  for (int e = 0; e < 3; e++) nc[e] = nf[e] / sc[e];
+  const int gmax = std::max(nf[0], std::max(nf[1], nf[2]));
+  const int gmax1 = gmax + 1, gstride = 9 * gmax1;
+  std::vector<T> gF(gstride, T(0)), gC(gstride, T(0));
+  for (int e = 0; e < 3; e++) {
+    for (int i = 0; i <= nf[e]; i++) gF[e * gmax1 + i] = (T)xf[e][i];
+    for (int i = 0; i <= nc[e]; i++) gC[e * gmax1 + i] = (T)xf[e][sc[e] * i];
+  }
+  LevelView<T> F, Cc;
+  for (int e = 0; e < 3; e++) {
+    F.n[e] = nf[e];
+    Cc.n[e] = nc[e];
+  }
+  set_slot_divs(F);
+  set_slot_divs(Cc);
+  F.nrhs = Cc.nrhs = 1;
+  F.S = (long)(nf[0] + 1) * (nf[1] + 1) * (nf[2] + 1);
+  Cc.S = (long)(nc[0] + 1) * (nc[1] + 1) * (nc[2] + 1);
+  F.ncell = (long)nf[0] * nf[1] * nf[2];
+  Cc.ncell = (long)nc[0] * nc[1] * nc[2];
+  F.gstride = Cc.gstride = gstride;
+  F.gmax1 = Cc.gmax1 = gmax1;
+  F.active = Cc.active = nullptr;
+  F.op = Cc.op = nullptr;
+  T *dgF, *dgC, *dw;
+  C_t<T>*dfine, *dcf, *dcu;
+  CK(M.get(&dgF, gstride * sizeof(T)));
+  CK(M.get(&dgC, gstride * sizeof(T)));
+  CK(M.get(&dw, 3 * gmax1 * sizeof(T)));
+  CK(M.get(&dfine, 3 * F.S * sizeof(C_t<T>)));
+  CK(M.get(&dcf, 3 * Cc.S * sizeof(C_t<T>)));
+  CK(M.get(&dcu, 3 * Cc.S * sizeof(C_t<T>)));
+  CK(cudaMemcpy(dgF, gF.data(), gstride * sizeof(T), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dgC, gC.data(), gstride * sizeof(T), cudaMemcpyHostToDevice));
+  const long nin = 3 * (dir == 0 ? F.S : Cc.S), nout = 3 * (dir == 0 ? Cc.S : F.S);
+  std::vector<C_t<T>> hin(nin), hout(nout);
+  for (long i = 0; i < nin; i++) hin[i] = mk<T>((T)in[2 * i], (T)in[2 * i + 1]);
+  for (long i = 0; i < nout; i++) hout[i] = mk<T>((T)out[2 * i], (T)out[2 * i + 1]);
+  F.geo = dgF;
+  Cc.geo = dgC;
+  F.u = F.r = dfine;
+  F.f = nullptr;
+  Cc.f = dcf;
+  Cc.u = dcu;
+  launch_xfer_weights<T>(F, Cc, sc, 1, dw, 0);
+  F.xw = dw;
+  if (dir == 0) {
+    CK(cudaMemcpy(dfine, hin.data(), nin * sizeof(C_t<T>), cudaMemcpyHostToDevice));
+    launch_restrict<T>(F, Cc, sc, 0);
+  } else {
+    CK(cudaMemcpy(dcu, hin.data(), nin * sizeof(C_t<T>), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dfine, hout.data(), nout * sizeof(C_t<T>), cudaMemcpyHostToDevice));
+    launch_prolong<T>(F, Cc, sc, 0);
+  }
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(hout.data(), dir == 0 ? dcf : dfine, nout * sizeof(C_t<T>), cudaMemcpyDeviceToHost));
+  for (long i = 0; i < nout; i++) {
+    out[2 * i] = (double)hout[i].x;
+    out[2 * i + 1] = (double)hout[i].y;
+  }
+  return EMMI_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -1851,6 +1924,22 @@ int emmi_level_residual(const int n[3], const double* x1, const double* x2, cons
   return prec == EMMI_PREC_FP64
              ? level_op<double>(n, x1, x2, x3, cells, omega, 0, 0, uc, f, r, norm)
              : level_op<float>(n, x1, x2, x3, cells, omega, 0, 0, uc, f, r, norm);
+}
+
+int emmi_level_transfer(const int nf[3], const double* x1, const double* x2, const double* x3,
+                        const int sc[3], int prec, int dir, const double* in, double* out) {
+  if (!nf || !x1 || !x2 || !x3 || !sc || !in || !out || dir < 0 || dir > 1) {
+    set_err("emmi_level_transfer: bad argument");
+    return EMMI_EINVAL;
+  }
+  for (int e = 0; e < 3; e++)
+    if ((sc[e] != 1 && sc[e] != 2) || nf[e] < 2 || nf[e] % sc[e] != 0) {
+      set_err("emmi_level_transfer: sc must be 1 or 2 and divide n (n >= 2)");
+      return EMMI_EINVAL;
+    }
+  const double* xf[3] = {x1, x2, x3};
+  return prec == EMMI_PREC_FP64 ? level_xfer<double>(nf, xf, sc, dir, in, out)
+                                : level_xfer<float>(nf, xf, sc, dir, in, out);
 }
 
 int emmi_level_smooth(const int n[3], const double* x1, const double* x2, const double* x3,

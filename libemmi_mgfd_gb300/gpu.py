@@ -410,6 +410,21 @@ def level_smooth(n, x, cells, omega, u, f, direction, prec=PREC_FP64, iter=0):
     return u
 
 
+def level_transfer(n, x, sc, inp, out, direction, prec=PREC_FP64):
+    """One grid transfer between a level of n cells (node coordinates x) and
+    the level coarsened by sc: direction 0 restricts the fine field inp to the
+    coarse level (returned), 1 returns out + the prolongation of the coarse
+    inp (out: the fine field)."""
+    n3 = (C.c_int * 3)(*[int(v) for v in n])
+    s3 = (C.c_int * 3)(*[int(v) for v in sc])
+    xs = [np.ascontiguousarray(v, np.float64) for v in x]
+    inp = np.ascontiguousarray(inp, np.complex128)
+    out = np.ascontiguousarray(out, np.complex128).copy()
+    _check(lib().emmi_level_transfer(n3, _p(xs[0]), _p(xs[1]), _p(xs[2]), s3, prec,
+                                     int(direction), _p(inp), _p(out)), "emmi_level_transfer")
+    return out
+
+
 def build_gradient(nxyz, o, d, idxpar, preco, Ef, Ea, rho11, rho33, bathy, src, rec,
                    dsmute=800.0, drmute=200.0):
     """Gradient w.r.t. ln(rho) summed over shots on the device.

@@ -106,3 +106,32 @@ def test_sweep_reduces_residual():
         u = G.level_smooth(n, x, cells, om, u, f, d, prec=G.PREC_FP64)
     r1 = np.linalg.norm(G.level_residual(n, x, cells, om, u, f, prec=G.PREC_FP64)[0])
     assert r1 < 0.5 * r0
+
+
+XFER = [((8, 6, 10), (1, 2, 2)), ((12, 12, 12), (2, 1, 2)), ((16, 8, 4), (2, 2, 1)),
+        ((8, 8, 8), (2, 2, 2))]
+
+
+@gpu
+@pytest.mark.parametrize("n,sc", XFER)
+@pytest.mark.parametrize("prec", [0, 1])
+def test_restriction_and_prolongation(n, sc, prec):
+    """One restriction and one prolongation (emmi_level_transfer: the
+    solver's kernels with the level's weight table) against the oracle's
+    (src/gmg.c:1463-1573) on stretched coordinates, for the semi-coarsening
+    masks of the three hierarchies and full coarsening.  The coarse
+    coordinates are the fine ones sub-sampled, as the hierarchy builds them."""
+    G = _gpu()
+    n, x, raw, cells, om, u, f = random_level(n, seed=7)
+    nc = tuple(a // b for a, b in zip(n, sc))
+    xc = [np.asarray(x[e])[::sc[e]].copy() for e in range(3)]
+    rng = np.random.default_rng(8)
+    sc_n = 3 * (nc[0] + 1) * (nc[1] + 1) * (nc[2] + 1)
+    uc = rng.standard_normal(sc_n) + 1j * rng.standard_normal(sc_n)
+    fc_ref = O.restrict(n, x, nc, xc, sc, f)
+    fc = G.level_transfer(n, x, sc, f, np.zeros(sc_n, np.complex128), 0, prec)
+    pf_ref = O.prolong(n, x, nc, xc, sc, uc, u)
+    pf = G.level_transfer(n, x, sc, uc, u, 1, prec)
+    tol = 1e-14 if prec == G.PREC_FP64 else 2e-6
+    assert rel_err(fc, fc_ref) < tol
+    assert rel_err(pf, pf_ref) < tol
