@@ -865,71 +865,88 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
-// Factors of every line of one colour, for group blockIdx.y of the chunk:
-// the forward elimination of k_line_solve on records assembled in buf
-// (their right-hand sides unused), factors to fac + grp * gstride:
-//   FMT 0 (kFacF32): the record layout, 12 values per row;
-//   FMT 1 (kFacF16, T = float): L(p+i, p), i = 1..5, rounded to fp16 in
-//   planes LA (i = 1..4) and LB (i = 5), 1/d_p in fp32 (ID); an L value
-//   outside the fp16 range (or not finite) sets *ovf.
-template <typename T, int FMT>
-__global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m, long gstride,
-                                                               const T* __restrict__ buf,
-                                                               T* __restrict__ fac,
-                                                               int* __restrict__ ovf) {
+// band entries (lower, real) and diagonal of row type TT of node s: the
+// band part of assemble_row's record
+template <typename T, int D, int TT, int C>
+__device__ __forceinline__ void band_row(const LevelView<T>& L, const T* cells, const Geo<T>& G,
+                                         T wmu, int ta, int tb, int s, int row, T (&band)[5],
+                                         C_t<T>& diag) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
+  int P[3];
+  P[D] = (TT == 0) ? s - 1 : s;
+  P[A] = ta - (TT == 1 ? 1 : 0);
+  P[B] = tb - (TT == 3 ? 1 : 0);
+  EdgeCoef<T> e;
+  edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e, L.imu_vol);
+#pragma unroll
+  for (int j = 0; j < 5; j++) band[j] = 0;
+#define LINE_ENTRY(K)                                                         \
+  {                                                                           \
+    constexpr int off = line_off(D, TT, K);                                   \
+    if constexpr (off < 0) {                                                  \
+      if (row + off >= 0) band[5 + off] = e.c[K];                             \
+    }                                                                         \
+  }
+  LINE_ENTRY(0) LINE_ENTRY(1) LINE_ENTRY(2) LINE_ENTRY(3) LINE_ENTRY(4) LINE_ENTRY(5)
+  LINE_ENTRY(6) LINE_ENTRY(7) LINE_ENTRY(8) LINE_ENTRY(9) LINE_ENTRY(10) LINE_ENTRY(11)
+#undef LINE_ENTRY
+  diag = mk<T>(e.dre, e.dim);
+}
+
+// Factors of every line of one colour, for group blockIdx.y of the chunk,
+// straight from the operator: a thread assembles a node's band rows in
+// registers (band_row) and runs the forward elimination of k_line_solve on
+// them -- no band records through memory -- writing factors to
+// fac + grp * gstride:
+//   FMT 0 (kFacF32): the record layout, 12 values per row, L(p+i, p) for
+//   i = 1..5 and 1/d_p;
+//   FMT 1 (kFacF16, T = float): L(p+i, p) rounded to fp16 in planes LA
+//   (i = 1..4) and LB (i = 5), 1/d_p in fp32 (ID); an L value outside the
+//   fp16 range (or not finite) sets *ovf.
+// y and z lines: neighbouring lines are neighbouring slots, so a warp's cell
+// loads coalesce; x lines read theirs along each thread's line (uncoalesced,
+// still faster than assembling records: 15.4 against 23.2 ms for the 128^3
+// batch's set-up).
+template <typename T, int D, int FMT>
+__global__ void __launch_bounds__(kSolveThreads) k_line_factor_direct(LevelView<T> L, int pa,
+                                                                      int pb, long gstride,
+                                                                      T* __restrict__ fac,
+                                                                      int* __restrict__ ovf) {
+  constexpr int A = (D == 0) ? 1 : 0, B = (D == 2) ? 1 : 2;
   using V = typename Vec16<T>::V;
   constexpr int NP = kPlanes<T>;
-  __shared__ V ring[kRing][NP][kSolveThreads];
   const int grp = blockIdx.y;
-  const int tid = threadIdx.x;
-  const long l = blockIdx.x * (long)blockDim.x + tid;
-  if (l >= nl) return;
-  const V* base = reinterpret_cast<const V*>(buf) + (long)grp * m * NP * nl + l;
+  const LineGeom g = line_geom<D>(L.n, pa, pb);
+  const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (l >= g.nl) return;
+  const unsigned lq = (unsigned)l / (unsigned)g.la;
+  const int ta = g.fa + 2 * (int)((unsigned)l - lq * (unsigned)g.la), tb = g.fb + 2 * (int)lq;
+  const T* cells = L.cells + (long)op_of(L, grp) * 4 * L.ncell;
+  const Geo<T> G{L.geo + (long)op_of(L, grp) * L.gstride, L.gmax1};
+  const T wmu = L.wmu[grp];
+  const int m = g.m, nd = g.nd;
+  const long nl = g.nl;
   V* fout = reinterpret_cast<V*>(fac + (long)grp * gstride) + l;
   const long rs = NP * nl;
   HalfFac hf{};
   if constexpr (FMT == kFacF16) hf = half_fac(fac + (long)grp * gstride, m, nl);
   bool over = false;
-  auto issue = [&](int row) {
-    const V* src = base + (long)row * rs;
-    const int slot = row % kRing;
-#pragma unroll
-    for (int q = 0; q < NP; q++) cp_async16(&ring[slot][q][tid], src + q * nl);
-  };
   C_t<T> W[21];
 #pragma unroll
   for (int i = 0; i < 21; i++) W[i] = mk<T>(0, 0);
 #pragma unroll
   for (int i = 0; i < 5; i++) W[WI(i, i)] = mk<T>(1, 0);
-  for (int p = 0; p < kRing - 1; p++) {
-    if (p < m) issue(p);
-    cp_async_commit();
-  }
-  for (int row = 0; row < m + 5; row++) {
-    if (row < m) {
-      if (row + kRing - 1 < m) issue(row + kRing - 1);
-      cp_async_commit();
-      cp_async_wait<kRing - 1>();
-      T nxt[kRec];
-      const int slot = row % kRing;
-#pragma unroll
-      for (int q = 0; q < NP; q++) unpack16(ring[slot][q][tid], nxt + q * kLanes<T>);
-#pragma unroll
-      for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(nxt[j], 0);
-      W[WI(5, 5)] = mk<T>(nxt[5], nxt[6]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
-      W[WI(5, 5)] = mk<T>(1, 0);
-    }
+  // the arriving row sits in W[WI(5, .)]: eliminate pivot row - 5 and
+  // store its factors
+  auto step = [&](int row) {
     const C_t<T> id = crcp<T>(W[0]);
-    C_t<T> lq[6];
+    C_t<T> lqv[6];
 #pragma unroll
-    for (int i = 1; i < 6; i++) lq[i] = cmul<T>(W[WI(i, 0)], id);
+    for (int i = 1; i < 6; i++) lqv[i] = cmul<T>(W[WI(i, 0)], id);
 #pragma unroll
     for (int i = 1; i < 6; i++) {
 #pragma unroll
-      for (int j = 1; j <= i; j++) W[WI(i, j)] = cfms<T>(W[WI(i, j)], lq[i], W[WI(j, 0)]);
+      for (int j = 1; j <= i; j++) W[WI(i, j)] = cfms<T>(W[WI(i, j)], lqv[i], W[WI(j, 0)]);
     }
     const int piv = row - 5;
     if (piv >= 0) {
@@ -937,8 +954,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m, l
         T o[kRec];
 #pragma unroll
         for (int i = 1; i < 6; i++) {
-          o[2 * (i - 1)] = lq[i].x;
-          o[2 * (i - 1) + 1] = lq[i].y;
+          o[2 * (i - 1)] = lqv[i].x;
+          o[2 * (i - 1) + 1] = lqv[i].y;
         }
         o[10] = id.x;
         o[11] = id.y;
@@ -947,8 +964,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m, l
         __half2 h[5];
 #pragma unroll
         for (int i = 1; i < 6; i++) {
-          over |= !(fabsf(lq[i].x) <= 65504.f && fabsf(lq[i].y) <= 65504.f);
-          h[i - 1] = __floats2half2_rn(lq[i].x, lq[i].y);
+          over |= !(fabsf(lqv[i].x) <= 65504.f && fabsf(lqv[i].y) <= 65504.f);
+          h[i - 1] = __floats2half2_rn(lqv[i].x, lqv[i].y);
         }
         const long o = (long)piv * nl + l;
         hf.la[o] = make_uint4(h2u(h[0]), h2u(h[1]), h2u(h[2]), h2u(h[3]));
@@ -961,8 +978,46 @@ __global__ void __launch_bounds__(kSolveThreads) k_line_factor(long nl, int m, l
 #pragma unroll
       for (int j = 0; j <= i; j++) W[WI(i, j)] = W[WI(i + 1, j + 1)];
     }
+  };
+  T bd[5][5];
+  C_t<T> dg[5];
+  auto assemble = [&](auto tt, int s) {
+    constexpr int TT = decltype(tt)::value;
+    constexpr int C = (TT == 0) ? D : (TT <= 2 ? A : B);
+    band_row<T, D, TT, C>(L, cells, G, wmu, ta, tb, s, 5 * (s - 1) + TT, bd[TT], dg[TT]);
+  };
+  auto arrive = [&](auto tt, int s) {
+    constexpr int TT = decltype(tt)::value;
+#pragma unroll
+    for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(bd[TT][j], 0);
+    W[WI(5, 5)] = dg[TT];
+    step(5 * (s - 1) + TT);
+  };
+  // rows in record order: node s brings row 5(s-1) and, below the last
+  // node, its four transverse rows; a node's loads are issued together
+  for (int s = 1; s <= nd; s++) {
+    assemble(std::integral_constant<int, 0>(), s);
+    if (s < nd) {
+      assemble(std::integral_constant<int, 1>(), s);
+      assemble(std::integral_constant<int, 2>(), s);
+      assemble(std::integral_constant<int, 3>(), s);
+      assemble(std::integral_constant<int, 4>(), s);
+    }
+    arrive(std::integral_constant<int, 0>(), s);
+    if (s < nd) {
+      arrive(std::integral_constant<int, 1>(), s);
+      arrive(std::integral_constant<int, 2>(), s);
+      arrive(std::integral_constant<int, 3>(), s);
+      arrive(std::integral_constant<int, 4>(), s);
+    }
   }
-  cp_async_wait<0>();
+  // five unit rows flush the last pivots (rows m..m+4)
+  for (int row = m; row < m + 5; row++) {
+#pragma unroll
+    for (int j = 0; j < 5; j++) W[WI(5, j)] = mk<T>(0, 0);
+    W[WI(5, 5)] = mk<T>(1, 0);
+    step(row);
+  }
   if (over) atomicOr(ovf, 1);
 }
 
@@ -1220,24 +1275,21 @@ __global__ void __launch_bounds__(256) k_line_apply_rb(LevelView<T> L, int pa, i
 }
 
 template <typename T, int D>
-static void line_factor_d(const LevelView<T>& L, int color, T* buf, T* fac, int fmt, int* ovf,
+static void line_factor_d(const LevelView<T>& L, int color, T* fac, int fmt, int* ovf,
                           cudaStream_t st) {
   const int pa = color & 1, pb = (color >> 1) & 1;
   const long nl = line_count(L.n, D, color);
   if (nl == 0) return;
-  const long items = nl * L.n[D];
-  const int m = 5 * L.n[D] - 4;
   const long gstride = line_factor_elems(L.n, D, color, fmt);
-  dim3 g1((unsigned)((items + 255) / 256), L.nrhs);
-  k_line_assemble<T, D, false><<<g1, 256, 0, st>>>(L, pa, pb, buf);
-  dim3 g2((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
+  dim3 g((unsigned)((nl + kSolveThreads - 1) / kSolveThreads), L.nrhs);
   if constexpr (std::is_same<T, float>::value) {
     if (fmt == kFacF16) {
-      k_line_factor<T, kFacF16><<<g2, kSolveThreads, 0, st>>>(nl, m, gstride, buf, fac, ovf);
+      k_line_factor_direct<T, D, kFacF16><<<g, kSolveThreads, 0, st>>>(L, pa, pb, gstride, fac,
+                                                                       ovf);
       return;
     }
   }
-  k_line_factor<T, kFacF32><<<g2, kSolveThreads, 0, st>>>(nl, m, gstride, buf, fac, ovf);
+  k_line_factor_direct<T, D, kFacF32><<<g, kSolveThreads, 0, st>>>(L, pa, pb, gstride, fac, ovf);
 }
 
 // the fp16-factor substitution's block shapes (threads per block, ring
@@ -1364,15 +1416,6 @@ void init_line_kernels() {
     carve((const void*)k_line_subst_h<128, 6, 2>);
     carve((const void*)k_line_subst_h<64, 4, 2>);
     carve((const void*)k_line_subst_h<64, 8, 2>);
-    cudaFuncSetAttribute(k_line_factor<float, kFacF32>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_factor<float, kFacF16>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_line_factor<double, kFacF32>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_line_subst<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
   });
@@ -1394,12 +1437,11 @@ long line_factor_elems(const int n[3], int d, int color, int fmt) {
 }
 
 template <typename T>
-void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
-                        int fmt, int* ovf, cudaStream_t st) {
-  T* buf = reinterpret_cast<T*>(scratch);
-  if (d == 0) line_factor_d<T, 0>(L, color, buf, fac, fmt, ovf, st);
-  else if (d == 1) line_factor_d<T, 1>(L, color, buf, fac, fmt, ovf, st);
-  else line_factor_d<T, 2>(L, color, buf, fac, fmt, ovf, st);
+void launch_line_factor(const LevelView<T>& L, int d, int color, T* fac, int fmt, int* ovf,
+                        cudaStream_t st) {
+  if (d == 0) line_factor_d<T, 0>(L, color, fac, fmt, ovf, st);
+  else if (d == 1) line_factor_d<T, 1>(L, color, fac, fmt, ovf, st);
+  else line_factor_d<T, 2>(L, color, fac, fmt, ovf, st);
 }
 
 template <typename T>
@@ -2101,12 +2143,12 @@ void launch_zero(C_t<T>* p, long n, cudaStream_t st) {
   template void launch_zero<T>(C_t<T>*, long, cudaStream_t);
 EMMI_INST(float)
 EMMI_INST(double)
-template void launch_line_factor<float>(const LevelView<float>&, int, int, C_t<float>*, float*,
-                                        int, int*, cudaStream_t);
+template void launch_line_factor<float>(const LevelView<float>&, int, int, float*, int, int*,
+                                        cudaStream_t);
 template void launch_line_sweep_fac<float>(const LevelView<float>&, int, int, const float*,
                                            const int*, C_t<float>*, int, cudaStream_t, SweepShape);
-template void launch_line_factor<double>(const LevelView<double>&, int, int, C_t<double>*,
-                                         double*, int, int*, cudaStream_t);
+template void launch_line_factor<double>(const LevelView<double>&, int, int, double*, int, int*,
+                                         cudaStream_t);
 template void launch_line_sweep_fac<double>(const LevelView<double>&, int, int, const double*,
                                             const int*, C_t<double>*, int, cudaStream_t,
                                             SweepShape);

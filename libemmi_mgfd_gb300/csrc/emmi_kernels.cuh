@@ -37,16 +37,16 @@ long line_scratch_elems(const int n[3], int d, int nrhs);
 // stored LDL^T factors of the lines of one colour along d: T values per
 // operator group in format fmt (0: fp32 records, 12 values per row; 1: fp16
 // L and fp32 1/d, 7 values per row); launch_line_factor fills them for the
-// L.nrhs groups of L (L.op / L.wmu per group, u and f unused) through the
-// record scratch into fac + g * line_factor_elems and sets *ovf when an L
-// value does not fit fp16 (format 1); launch_line_sweep_fac then sweeps RHS
+// L.nrhs groups of L (L.op / L.wmu per group, u and f unused), the band rows
+// assembled in registers, into fac + g * line_factor_elems and sets *ovf
+// when an L value does not fit fp16 (format 1); launch_line_sweep_fac then sweeps RHS
 // r with the factors of group grp[r], rb holding (5 n_d - 4) * lines complex
 // values per RHS
 constexpr int kFacF32 = 0, kFacF16 = 1;
 long line_factor_elems(const int n[3], int d, int color, int fmt);
 template <typename T>
-void launch_line_factor(const LevelView<T>& L, int d, int color, C_t<T>* scratch, T* fac,
-                        int fmt, int* ovf, cudaStream_t st);
+void launch_line_factor(const LevelView<T>& L, int d, int color, T* fac, int fmt, int* ovf,
+                        cudaStream_t st);
 // block shapes of a stored-factor sweep: the fp16 substitution's variant
 // (subst_variant_threads lines per block, a cp.async ring of
 // subst_variant_ring rows; 0 = 64 x 6) and the right-hand-side kernel's

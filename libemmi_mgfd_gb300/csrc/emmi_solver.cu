@@ -587,9 +587,7 @@ static int build_line_factors(emmi_solver* s) {
     CK(cudaMemsetAsync(d_ovf, 0, sizeof(int), s->st));
     s->ngroups = ng;
     s->fac_bytes = bytes;
-    // factor every block once: records assembled into the scratch for
-    // `chunk` groups at a time (u and f of the level are read but their
-    // residual is not used)
+    // factor every block once, every group in one launch per colour
     std::vector<long> done;
     for (int h = 0; h < 3; h++)
       for (int l = 0; l + 1 < s->lmax; l++)
@@ -604,21 +602,10 @@ static int build_line_factors(emmi_solver* s) {
           V.op = s->d_gop;
           V.wmu = static_cast<const T*>(s->d_gwmu);
           V.active = nullptr;
-          for (int c = 0; c < 4; c++) {
-            const long per = line_factor_elems(s->hier[h][l].n, d, c, fmt);
-            for (int g0 = 0; g0 < ng; g0 += s->chunk) {
-              LevelView<T> W = V;
-              W.nrhs = std::min(s->chunk, ng - g0);
-              W.u += (long)g0 * 3 * V.S;
-              W.f += (long)g0 * 3 * V.S;
-              W.op += g0;
-              W.wmu += g0;
-              launch_line_factor<T>(W, d, c, (C_t<T>*)s->scratch,
-                                    static_cast<T*>(s->d_fac) + s->fac_off[hb][l][d][c] +
-                                        (long)g0 * per,
-                                    fmt, d_ovf, s->st);
-            }
-          }
+          V.nrhs = ng;
+          for (int c = 0; c < 4; c++)
+            launch_line_factor<T>(V, d, c, static_cast<T*>(s->d_fac) + s->fac_off[hb][l][d][c], fmt,
+                                  d_ovf, s->st);
         }
     CK(cudaGetLastError());
     int ovf = 0;
