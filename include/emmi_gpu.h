@@ -149,6 +149,20 @@ int emmi_solver_line_format(const emmi_solver *s);
  * it reads the volume-weighted invmur cells; the FP64 operator always reads
  * them (the reference's arithmetic). */
 int emmi_solver_geometric_weights(const emmi_solver *s);
+/* 1 when the complex64 level-0 residual of s stages its halos by tensor
+ * copies (emmi_options.staged and a tile that fits shared memory). */
+int emmi_solver_staged(const emmi_solver *s);
+/* Test hook of the staged residual's bounded waits (no counterpart in the
+ * reference): the staged residuals launched after the call give up a wait
+ * for a plane's copies after wait_cycles clocks (0: the default, about a
+ * second), and with stall_from >= 0 no copy of a plane at or beyond that
+ * index is issued, so the first wait for one runs out: the CTA records the
+ * failure, waits (with the full limit) for the copies it did issue and
+ * returns, the launches after it return at once, and the solve reports
+ * EMMI_ECUDA at its next norm check; stall_from = -1 issues every copy.
+ * Launches captured in the cycle graphs keep the settings of their capture:
+ * create s with use_graphs = 0 for the hook to reach its cycles. */
+int emmi_stencil_wait_hook(emmi_solver *s, long long wait_cycles, int stall_from);
 /* Number of kernel launches in the last solve. */
 long emmi_solver_last_launches(const emmi_solver *s);
 /* Device bytes held by the solver. */

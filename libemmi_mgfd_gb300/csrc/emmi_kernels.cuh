@@ -88,7 +88,8 @@ struct StencilArgs {
   int Ru, Rc;       // 256-byte rows of a u window and of a cell window
   int ncarr;        // cell arrays staged: 3 (sigma) or 4 (+ inverse permeability)
   unsigned uwin, cwin, slot;  // bytes: one u window, one cell window, one slot
-  long long wait;   // clocks a wait gives up after
+  long long wait;   // clocks a wait for a plane's copies gives up after
+  int stall = -1;   // test hook: thread 0 issues no copy from this plane on
 };
 struct StencilPlan {
   CUtensorMap tu, tc;
@@ -96,6 +97,8 @@ struct StencilPlan {
   bool ok = false;
 };
 long stencil_pad(long elems, int esize);
+// the wait limit (clocks, 0 = the default) and the test stall of a plan
+void stencil_hook(StencilPlan* P, long long wait, int stall);
 bool stencil_prepare(const LevelView<float>& V, long u_elems, long cell_elems, StencilPlan* out);
 void launch_residual_staged(const LevelView<float>& L, const StencilPlan& P, C_t<float>* rout,
                             double* norm2, cudaStream_t st);

@@ -1683,6 +1683,18 @@ int emmi_solver_line_factor_format(const emmi_solver* s) {
   return s && s->fac_on ? s->fac_fmt : -1;
 }
 int emmi_solver_geometric_weights(const emmi_solver* s) { return s && s->imu_vol ? 1 : 0; }
+int emmi_solver_staged(const emmi_solver* s) { return s && s->plan[0][0].ok ? 1 : 0; }
+
+int emmi_stencil_wait_hook(emmi_solver* s, long long wait_cycles, int stall_from) {
+  if (!s || wait_cycles < 0 || stall_from < -1) {
+    set_err("emmi_stencil_wait_hook: bad argument");
+    return EMMI_EINVAL;
+  }
+  for (int h = 0; h < 3; h++)
+    for (int l = 0; l < kMaxLev; l++)
+      if (s->plan[h][l].ok) stencil_hook(&s->plan[h][l], wait_cycles, stall_from);
+  return EMMI_OK;
+}
 int emmi_solver_line_format(const emmi_solver* s) {
   return s && (s->opt.line_sweep || s->opt.fused_level < s->lmax) ? s->lfmt : -1;
 }

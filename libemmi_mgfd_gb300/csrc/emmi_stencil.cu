@@ -123,7 +123,10 @@ __global__ void __launch_bounds__(kStThreads) k_residual_staged(
   // tensor copies land on 128-byte boundaries
   unsigned char* slot0 =
       sm_raw + ((128u - (st_su32(sm_raw) & 127u)) & 127u);
-  auto issue = [&](int p) {  // thread 0: the copies of plane p into its slot
+  // thread 0: the copies of plane p into its slot; false (nothing issued)
+  // from the test hook's stall plane on
+  auto issue = [&](int p) -> bool {
+    if (a.stall >= 0 && p >= a.stall) return false;
     const int sl = slot_of(p);
     const uint32_t b = st_su32(&bar[sl]);
     unsigned char* base = slot0 + (size_t)sl * a.slot;
@@ -134,14 +137,13 @@ __global__ void __launch_bounds__(kStThreads) k_residual_staged(
     if (cells)
       for (int A = 0; A < a.ncarr; A++)
         st_tma_2d(st_su32(base + 3 * a.uwin + A * a.cwin), &tc, (int)(cfirst(A, p) >> 6), b);
+    return true;
   };
   // planes k0-1 .. k1 (those inside the grid) are staged; p is computed with
   // p-1..p+1 in the ring
-  int issued = pfirst - 1;
-  if (tid == 0) {
-    for (int p = pfirst; p <= min(pfirst + kStRing - 2, plast); p++) issue(p);
-    issued = min(pfirst + kStRing - 2, plast);
-  }
+  int issued = pfirst - 1;  // thread 0: the last plane whose copies are in flight or landed
+  if (tid == 0)
+    for (int p = pfirst; p <= min(pfirst + kStRing - 2, plast) && issue(p); p++) issued = p;
   const float wmu = L.wmu[rhs];
   const Geo<float> G{L.geo + (long)op * L.gstride, L.gmax1};
   const float2* f = L.f ? L.f + (long)rhs * 3 * S : nullptr;
@@ -152,16 +154,17 @@ __global__ void __launch_bounds__(kStThreads) k_residual_staged(
     // every plane up to k+1 landed; plane k+2 goes into the slot plane k-2 left
     const int need = min(k + 1, plast);
     bool ok = true;
-    for (int p = waited + 1; p <= need && ok; p++) ok = st_mbar_wait(st_su32(&bar[slot_of(p)]), use_of(p), a.wait);
+    for (int p = waited + 1; p <= need && ok; p++) {
+      ok = st_mbar_wait(st_su32(&bar[slot_of(p)]), use_of(p), a.wait);
+      if (ok) waited = p;  // on a failure: waited is the last plane seen landed
+    }
     if (!ok) failed = 1;
-    waited = need;
     __syncthreads();
     if (failed) break;
     if (tid == 0 && k + kStRing - 2 <= plast && k + kStRing - 2 > issued) {
       // the slot's previous contents were read through the generic proxy
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      issue(k + kStRing - 2);
-      issued = k + kStRing - 2;
+      if (issue(k + kStRing - 2)) issued = k + kStRing - 2;
     }
     // plane pointers: u of component c at plane k+dz, cells of array A at
     // cell plane k+dz, each shifted so that [j*X + i] / [j*n0 + i] address
@@ -295,8 +298,9 @@ __global__ void __launch_bounds__(kStThreads) k_residual_staged(
     if (tid == 0) {
       atomicExch(err, 1);
       // copies issued and not yet seen land before the shared memory goes
+      // (the full limit: an issued copy does land)
       for (int p = waited + 1; p <= issued; p++)
-        st_mbar_wait(st_su32(&bar[slot_of(p)]), use_of(p), a.wait);
+        st_mbar_wait(st_su32(&bar[slot_of(p)]), use_of(p), kStWait);
     }
     return;
   }
@@ -356,6 +360,11 @@ int* stencil_err() {
   static std::once_flag once;
   std::call_once(once, [] { cudaGetSymbolAddress((void**)&p, g_stencil_err); });
   return p;
+}
+
+void stencil_hook(StencilPlan* P, long long wait, int stall) {
+  P->args.wait = wait > 0 ? wait : kStWait;
+  P->args.stall = stall;
 }
 
 long stencil_pad(long elems, int esize) {

@@ -345,6 +345,18 @@ class Solver:
         return bool(lib().emmi_solver_geometric_weights(self._h))
 
     @property
+    def staged(self) -> bool:
+        """True when the complex64 level-0 residual stages its halos by
+        tensor copies."""
+        return bool(lib().emmi_solver_staged(self._h))
+
+    def stencil_wait_hook(self, wait_cycles: int = 0, stall_from: int = -1):
+        """Test hook of the staged residual's bounded waits (see
+        emmi_stencil_wait_hook; reaches the cycles with use_graphs=0)."""
+        _check(lib().emmi_stencil_wait_hook(self._h, C.c_longlong(wait_cycles), int(stall_from)),
+               "emmi_stencil_wait_hook")
+
+    @property
     def line_format(self) -> int:
         """Multipliers of the one-launch line sweep: 1 fp16, 0 working
         precision, -1 the three-launch sweep."""

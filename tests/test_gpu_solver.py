@@ -606,3 +606,27 @@ def test_skipped_post_smoothing_converges_to_the_same_field(golden, precision):
     # fewer launches per cycle without the two levels' post-smoothing
     per = {m: out[m][3] / out[m][2]["cycles"] for m in (0, 3)}
     assert per[3] < per[0], per
+
+
+@gpu
+def test_staged_residual_wait_that_runs_out_reports_and_recovers(golden):
+    """The staged residual's bounded waits: with the test hook no tensor copy
+    of plane 3 or beyond is issued and a wait gives up after 2e6 clocks
+    (about a millisecond), so the first level-0 residual's wait for plane 3
+    runs out; the CTA waits for the copies it did issue and returns, the
+    solve reports the failure at its norm check, and with the hook cleared
+    the same solver on the same GPU solves to tolerance."""
+    g = golden("tiny_layered")
+    G = _G()
+    n, xx, raw, om = golden_level(g)
+    b = g["b_f0"][None]
+    s = G.Solver(n, *[v.astype(np.float32) for v in xx], raw[None], np.array([om], np.float32),
+                 options=G.Options(precision=G.PREC_MIXED, ncycle=60, tol=1e-8, use_graphs=0))
+    assert s.staged
+    s.stencil_wait_hook(2_000_000, 3)
+    with pytest.raises(RuntimeError, match="staged residual"):
+        s.solve(b)
+    s.stencil_wait_hook(0, -1)
+    x, h, st = s.solve(b)
+    assert st[0]["status"] == "ok" and st[0]["rel"] <= 1e-8, st
+    s.close()
