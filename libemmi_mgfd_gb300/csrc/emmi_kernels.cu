@@ -2095,7 +2095,10 @@ __global__ void __launch_bounds__(256) k_coarsen(const T* __restrict__ fine, int
   const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (id >= ncc) return;
   const long arr = blockIdx.y;  // rhs*4 + which
-  const int i = (int)(id % nc0), j = (int)((id / nc0) % nc1), k = (int)(id / ((long)nc0 * nc1));
+  // 32-bit decode (a level has fewer than 2^31 cells)
+  const unsigned t = (unsigned)id / (unsigned)nc0;
+  const int i = (int)((unsigned)id - t * (unsigned)nc0);
+  const int j = (int)(t % (unsigned)nc1), k = (int)(t / (unsigned)nc1);
   const int i0 = sc0 == 2 ? 2 * i : i, i1 = sc0 == 2 ? 2 * i + 1 : i;
   const int j0 = sc1 == 2 ? 2 * j : j, j1 = sc1 == 2 ? 2 * j + 1 : j;
   const int k0 = sc2 == 2 ? 2 * k : k, k1 = sc2 == 2 ? 2 * k + 1 : k;

@@ -107,7 +107,10 @@ __global__ void k_weight_cells(const float* __restrict__ raw, const double* __re
   const long id = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (id >= ncell) return;
   const int op = blockIdx.y;
-  const int i = (int)(id % n0), j = (int)((id / n0) % n1), k = (int)(id / ((long)n0 * n1));
+  // 32-bit decode (a level has fewer than 2^31 cells)
+  const unsigned t = (unsigned)id / (unsigned)n0;
+  const int i = (int)((unsigned)id - t * (unsigned)n0);
+  const int j = (int)(t % (unsigned)n1), k = (int)(t / (unsigned)n1);
   const double* g = geo + (long)op * gstride;
   const double vol = g[3 * gmax1 + i] * g[4 * gmax1 + j] * g[5 * gmax1 + k];
   for (int a = 0; a < 4; a++) {
