@@ -374,7 +374,8 @@ long stencil_pad(long elems, int esize) {
 
 // tile geometry and tensor maps for the residual of level view V (all of
 // its RHS, the arrays V.u and V.cells padded by stencil_pad); false when the
-// level cannot be staged (too wide a row for a slot, no encoder)
+// level is not staged (too wide a row for a tile that keeps every thread
+// busy, no encoder)
 bool stencil_prepare(const LevelView<float>& V, long u_elems, long cell_elems, StencilPlan* out) {
   const int X = V.n[0] + 1, Y = V.n[1] + 1, Z = V.n[2] + 1;
   const int n0 = V.n[0];
@@ -395,7 +396,10 @@ bool stencil_prepare(const LevelView<float>& V, long u_elems, long cell_elems, S
       break;
     }
   }
-  if (!TY) return false;
+  // wide rows leave only thin tiles in shared memory: when the tile is cut
+  // below 16 rows (or the grid's rows) and no longer gives every thread a
+  // slot per plane, the plain kernel does better
+  if (!TY || (TY < std::min(16, Y) && (long)TY * (X - 1) < kStThreads)) return false;
   a.TY = TY;
   a.KZ = 32;
   a.ntj = (Y + TY - 1) / TY;
