@@ -451,8 +451,8 @@ __device__ __forceinline__ bool line_item_fd(const LineGeom& g, const LineDiv& v
   return true;
 }
 
-// RES false: the band entries only (factor set-up; the residual slot is 0)
-template <typename T, int D, int TT, int C, bool RES = true>
+// the record of row type TT of node s: band entries, diagonal, residual
+template <typename T, int D, int TT, int C>
 __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>* u,
                                              const C_t<T>* f, const T* cells, const Geo<T>& G,
                                              T wmu, int ta, int tb, int s, int row,
@@ -465,13 +465,8 @@ __device__ __forceinline__ void assemble_row(const LevelView<T>& L, const C_t<T>
   P[B] = tb - (TT == 3 ? 1 : 0);
   const int sl = P[0] + (L.n[0] + 1) * (P[1] + (L.n[1] + 1) * P[2]);  // 32-bit slot
   EdgeCoef<T> e;
-  C_t<T> r = mk<T>(0, 0);
-  if constexpr (RES) {
-    const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
-    r = csub<T>(f[C * (int)L.S + sl], au);
-  } else {
-    edge_coef<T, C>(L.n, P, cells + (long)C * L.ncell, cells + 3 * L.ncell, G, wmu, e, L.imu_vol);
-  }
+  const C_t<T> au = apply_row<T, C>(L, u, cells, G, wmu, P, sl, ss, e);
+  const C_t<T> r = csub<T>(f[C * (int)L.S + sl], au);
   T band[5] = {0, 0, 0, 0, 0};
 #define LINE_ENTRY(K)                                                         \
   {                                                                           \
@@ -506,8 +501,8 @@ __device__ __forceinline__ long line_slot(const int n[3], long S, int ta, int tb
 }
 
 // one thread per (line, node) and its five rows: y and z lines, whose
-// neighbouring lines are neighbouring slots (RES false: band entries only)
-template <typename T, int D, bool RES = true>
+// neighbouring lines are neighbouring slots
+template <typename T, int D>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(LevelView<T> L,
                                                                               int pa, int pb,
                                                                               T* __restrict__ buf) {
@@ -532,12 +527,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_line_assemble(L
   const long ps = g.nl;
   const int r0 = 5 * (s - 1);
   auto rec = [&](int row) { return base + (long)row * kPlanes<T> * g.nl + l; };
-  assemble_row<T, D, 0, D, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0), ps);
+  assemble_row<T, D, 0, D>(L, u, f, cells, G, wmu, ta, tb, s, r0, ss, rec(r0), ps);
   if (s < g.nd) {
-    assemble_row<T, D, 1, A, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1), ps);
-    assemble_row<T, D, 2, A, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2), ps);
-    assemble_row<T, D, 3, B, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3), ps);
-    assemble_row<T, D, 4, B, RES>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4), ps);
+    assemble_row<T, D, 1, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 1, ss, rec(r0 + 1), ps);
+    assemble_row<T, D, 2, A>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 2, ss, rec(r0 + 2), ps);
+    assemble_row<T, D, 3, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 3, ss, rec(r0 + 3), ps);
+    assemble_row<T, D, 4, B>(L, u, f, cells, G, wmu, ta, tb, s, r0 + 4, ss, rec(r0 + 4), ps);
   }
 }
 
