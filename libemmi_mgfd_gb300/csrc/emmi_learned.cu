@@ -299,7 +299,11 @@ __global__ void __launch_bounds__(kTcThreads) k_ls_conv(ConvArgs a, const uint4*
   __shared__ volatile int failed;
   const int b = blockIdx.y;
   if (a.mask && !a.mask[b]) return;
-  if (*(volatile int*)err) return;  // an earlier CTA gave up: the launch has failed
+  // an earlier CTA gave up: the launch has failed (one read for the CTA, so
+  // that every thread leaves or stays)
+  if (threadIdx.x == 0) failed = *(volatile int*)err ? 1 : 0;
+  __syncthreads();
+  if (failed) return;
   const int col = blockIdx.x % a.ncol, chunk = blockIdx.x / a.ncol;
   const int k0 = chunk * kTcPlanes;
   const int k1 = min(k0 + kTcPlanes, a.Z - 1);  // planes [k0, k1) are computed

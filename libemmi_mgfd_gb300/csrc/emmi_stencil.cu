@@ -88,7 +88,6 @@ __global__ void __launch_bounds__(kStThreads) k_residual_staged(
   __shared__ volatile int failed;
   const int rhs = blockIdx.y;
   if (L.active && !L.active[rhs]) return;
-  if (*(volatile int*)err) return;  // an earlier CTA gave up: the launch has failed
   const int X = L.n[0] + 1, Y = L.n[1] + 1, Z = L.n[2] + 1;
   const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
   const int XY = X * Y;
@@ -102,11 +101,14 @@ __global__ void __launch_bounds__(kStThreads) k_residual_staged(
   const int tid = threadIdx.x;
 
   if (tid == 0) {
+    // an earlier CTA gave up: the launch has failed (one read for the CTA,
+    // so that every thread leaves or stays)
+    failed = *(volatile int*)err ? 1 : 0;
     for (int i = 0; i < kStRing; i++) st_mbar_init(st_su32(&bar[i]), 1);
-    failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
+  if (failed) return;
 
   // element offsets of the windows of plane p (u: component c; cells: array A)
   auto ufirst = [&](int c, int p) -> long {
