@@ -6,7 +6,9 @@ and against FP64 solves of the same batches.
   * the 128^3 log-normal configuration: all 25 shots, complex64 cycles with
     the learned correction and FP64 refinement to 1e-8, against an FP64
     solve of the batch to 1e-12 (every shot) and against the reference's
-    receiver data of shots 1 and 13 (solved by the reference to 1e-10);
+    receiver data of shots 1 and 13 (solved by the reference to 1e-10); and
+    the benchmark's cycle (no post-smoothing on levels 0 and 1) against the
+    same reference data;
   * the VTI / bathymetry configuration (25 shots x 2 frequencies) on the
     48x48x64 mesh the reference can build for it: shots 1 and 13 at both
     frequencies against the reference's receiver data;
@@ -57,10 +59,11 @@ def _batch(s, shots=None):
                 rho_water=np.float32(m.rho_water()), nf=nf)
 
 
-def _model(s, b, precision, tol, ncycle=200, learned=None):
+def _model(s, b, precision, tol, ncycle=200, learned=None, skip_post=0):
     from libemmi_mgfd_gb300 import gpu as G
     sv = G.Solver(s.n, *b["X"], b["cells"], b["omega"], op=b["op"],
-                  options=G.Options(precision=precision, tol=tol, ncycle=ncycle),
+                  options=G.Options(precision=precision, tol=tol, ncycle=ncycle,
+                                    skip_post=skip_post),
                   rho_water=b["rho_water"])
     if learned is not None:
         sv.set_learned(learned)
@@ -98,6 +101,28 @@ def test_config3_batch_receivers_against_fp64_and_reference(golden):
               f"learned+mixed {a1:.2e} / {p1:.2e} deg, FP64 {a2:.2e} / {p2:.2e} deg")
         assert a1 < 1e-4 and p1 < 0.05, (k, a1, p1)
         assert a2 < 1e-4 and p2 < 0.05, (k, a2, p2)
+
+
+@gpu
+def test_config3_bench_cycle_receivers_match_reference(golden):
+    """The benchmark's own configuration: the 25 shots at 1 Hz, complex64
+    cycles without the post-smoothing of levels 0 and 1 (skip_post = 3) and
+    the learned correction trained on residuals of that cycle, FP64
+    refinement to 1e-8, against the reference's receiver data of shots 1
+    and 13 (solved by the reference to 1e-10)."""
+    from libemmi_mgfd_gb300 import gpu as G
+    from libemmi_mgfd_gb300 import learned as LS
+    g = golden("c3_lognormal_128_ref")
+    s = W.config3(128)
+    b = _batch(s)
+    ch = list(s.chrec)
+    tr = LS.train(n=48, models=6, per_rhs=6, steps=300, lr=3e-3, seed=100, skip_post=3)
+    d, st = _model(s, b, G.PREC_MIXED, 1e-8, ncycle=100, learned=tr["weights"], skip_post=3)
+    assert all(q["status"] == "ok" and q["rel"] <= 1e-8 for q in st), st
+    for k in g["shots"]:
+        a1, p1 = receiver_parity(d[k - 1], g[f"s{k}_dcal"], ch)
+        print(f"shot {k} vs reference: bench cycle + learned {a1:.2e} / {p1:.2e} deg")
+        assert a1 < 1e-4 and p1 < 0.05, (k, a1, p1)
 
 
 @gpu
